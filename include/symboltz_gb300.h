@@ -1,0 +1,143 @@
+/* symboltz_gb300: C-ABI of the GB300 perturbation + line-of-sight engine.
+ *
+ * Drop-in for the hot path of hersle/SymBoltz.jl.  Each entry point names the reference
+ * function (file:line inside the SymBoltz.jl repository) whose behaviour it replaces; the
+ * Julia/Python bindings that call these are shown in INTEGRATION.md.
+ *
+ * Conventions: plain pointers and sizes; host pointers unless the name ends in _device;
+ * integer status returns (0 = ok, < 0 = argument/CUDA errors, see SBZ_ERR_*); per-mode solver
+ * failures never abort a call: they are reported per mode (SBZ_MAXITERS, SBZ_DTMIN,
+ * SBZ_NONFINITE) exactly where the reference warns and returns a non-success retcode
+ * (src/solve.jl:557-564).  One CUDA stream per problem handle; a handle is not re-entrant.
+ * Units follow the reference: τ in 1/H0, k in H0/c (src/SymBoltz.jl:23-28).
+ */
+#ifndef SYMBOLTZ_GB300_H
+#define SYMBOLTZ_GB300_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define SBZ_OK 0
+#define SBZ_MAXITERS 1     /* more steps than opts.maxiters */
+#define SBZ_DTMIN 2        /* step size underflow */
+#define SBZ_NONFINITE 3    /* NaN/Inf in the solution or its error estimate */
+#define SBZ_ERR_ARG (-1)
+#define SBZ_ERR_CUDA (-2)
+#define SBZ_ERR_NOMEM (-3)
+#define SBZ_ERR_STATE (-4)
+
+/* ---- stage linear solves ---- */
+#define SBZ_FP64 0   /* structured LU of (1/(hγ) - J) in FP64 */
+#define SBZ_MIXED 1  /* structured LU in FP32 + FP64 iterative refinement (FP64 residuals) */
+
+/* ---- perturbation outputs ---- */
+#define SBZ_OUT_SOURCES 0  /* k*S_T, k^2*S_E, S_psi at the saved times   (src/models/cosmologies.jl:99-105) */
+#define SBZ_OUT_DELTA_M 1  /* total matter Δ_m(τ0)                         (src/observables/fourier.jl:39-52) */
+#define SBZ_OUT_STATE 2    /* full perturbation state at the saved times   (solvept output_func = identity) */
+
+/* Cosmological parameters of one cosmology: parameters_Planck18 keys (src/parameters.jl:1-21). */
+typedef struct sbz_params {
+  double h, Omega_c, Omega_b, T0, Neff, YHe, ln_As1e10, ns;
+  double m_nu_eV;  /* mass of each massive neutrino (eV) */
+  double N_nu;     /* number of degenerate massive neutrinos */
+} sbz_params;
+
+/* Model options: ΛCDM(lmax, Hswitch, Heswitch, reionization) (src/models/cosmologies.jl:27-48). */
+typedef struct sbz_model {
+  int lmax_gamma;  /* photon temperature + polarisation hierarchy (>= 3) */
+  int lmax_nu;     /* massless neutrinos (>= 3) */
+  int lmax_h;      /* massive neutrinos (>= 3) */
+  int nx_h;        /* massive-neutrino momentum bins (0 = no massive species, max 8) */
+  int Hswitch, Heswitch, reionization;
+} sbz_model;
+
+/* Solver options: CosmologyProblem(ivspan) + solve(bgopts, ptopts) (src/solve.jl:129-134,380-386). */
+typedef struct sbz_opts {
+  double bg_rtol, bg_atol;  /* default 1e-7 */
+  double pt_rtol, pt_atol;  /* default 1e-5 */
+  double tau_ini, tau_max;  /* background span, default (1e-6, 100) */
+  int64_t maxiters;         /* default 100000 */
+  int precision;            /* SBZ_FP64 or SBZ_MIXED */
+  int refine_iters;         /* FP64 refinement sweeps per stage solve (SBZ_MIXED), default 1 */
+  int table_points;         /* background coefficient table nodes, default 8192 */
+  int warps_per_block;      /* 0 = autotuned */
+} sbz_opts;
+
+typedef struct sbz_problem sbz_problem;
+typedef struct sbz_bessel sbz_bessel;
+
+void sbz_default_opts(sbz_opts* o);
+const char* sbz_last_error(void);
+
+/* Momentum bins x_i and weights W_i for ∫dx x² f0(x) g(x) (src/models/neutrinos.jl:55-60). */
+int sbz_momentum_quadrature(int N, double* x, double* W);
+
+/* CosmologyProblem(M, pars) for n_cosmo parameter sets sharing one model (src/solve.jl:129-236;
+ * several sets replace the reference's parameter_updater loop, src/solve.jl:272-307). */
+int sbz_problem_create(const sbz_model* m, const sbz_params* p, int n_cosmo, const sbz_opts* o, sbz_problem** out);
+void sbz_problem_destroy(sbz_problem* pb);
+int sbz_problem_nstate(const sbz_problem* pb);
+
+/* solvebg (src/solve.jl:427-435) with the a = 1 callback (src/solve.jl:158-203): τ0, κ0, τrec and
+ * status per cosmology (arrays of n_cosmo, any may be NULL).  Also builds and uploads the
+ * background coefficient tables read by the perturbation kernels. */
+int sbz_solve_bg(sbz_problem* pb, double* tau0, double* kappa0, double* taurec, int* status);
+/* Background solution knots of one cosmology (bgsol.t and unknowns); returns the count. */
+int sbz_bg_knots(const sbz_problem* pb, int cosmo, int cap, double* tau, double* y5);
+/* Derived background quantities (a, ℋ, κ̇, κ, v, v̇, c_s², Xe, Tb) at n times. */
+int sbz_bg_eval(const sbz_problem* pb, int cosmo, int n, const double* tau, double* out9);
+
+/* Background coefficients as the perturbation kernels read them (Hermite interpolation of the
+ * per-cosmology table): a, ℋ, κ̇, c_s², e^{-κ}, κ̈, κ⃛ at n times (thermodynamics observables of
+ * src/models/baryons.jl:155-183). */
+int sbz_bg_coefficients(const sbz_problem* pb, int cosmo, int n, const double* tau, double* out7);
+
+/* solvept (src/solve.jl:543-569) over nk modes: mode i belongs to cosmology cosmo[i] (NULL = all 0),
+ * has wavenumber ks[i] and initial time tau_ini[i] (clamped to the background span, src/solve.jl:527).
+ * Saved times: taus[c*ntau + j] for cosmology c (saveat).  out layout:
+ *   SBZ_OUT_SOURCES: out[(i*ntau + j)*3 + s]; SBZ_OUT_DELTA_M: out[i]; SBZ_OUT_STATE: out[(i*ntau + j)*n + m].
+ * status[i] per mode (may be NULL); steps[2i], steps[2i+1] = accepted, rejected (may be NULL). */
+int sbz_solve_pt(sbz_problem* pb, int nk, const int* cosmo, const double* ks, const double* tau_ini,
+                 int ntau, const double* taus, int output, double* out, int* status, int64_t* steps);
+/* Same with device pointers, enqueued on the problem's stream (no host synchronisation). */
+int sbz_solve_pt_device(sbz_problem* pb, int nk, const int* cosmo, const double* ks, const double* tau_ini,
+                        int ntau, const double* taus, int output, double* out, int* status, int64_t* steps);
+
+/* The perturbation right-hand side f = J(τ) y and ∂f/∂τ as the GPU integrator evaluates them, for
+ * nk (cosmology, k, τ, y) points: the counterpart of the generated ODE function prob.pt.f and its
+ * time derivative (src/solve.jl:227).  y, f, dfdtau: [i*n + m] in the library's state ordering
+ * (see sbz_layout.hpp: Φ, δc, θc, δb, θb, F0-2, G0-2, F3.., G3.., N0.., ψ_{j,l}). */
+int sbz_pt_rhs(sbz_problem* pb, int nk, const int* cosmo, const double* ks, const double* taus, const double* y,
+               double* f, double* dfdtau);
+
+/* spectrum_matter(prob, ks) (src/observables/fourier.jl:79-101): P(k, τ0) = P0(k) Δ_m² with
+ * τ_ini = min(kτini/k, τinimax); kτini = 1e-2, τinimax = 1e-4 by default. */
+int sbz_spectrum_matter(sbz_problem* pb, int nk, const int* cosmo, const double* ks, double ktau_ini,
+                        double tau_ini_max, double* Pk, int* status);
+/* spectrum_primordial (src/observables/fourier.jl:14-30) of one cosmology. */
+int sbz_spectrum_primordial(const sbz_problem* pb, int cosmo, int nk, const double* ks, double* P0);
+
+/* SphericalBesselCache(ls; xmax, dx, hermite) (src/observables/angular.jl:18-26), built on the GPU. */
+int sbz_bessel_create(int nl, const int* ls, double xmax, double dx, int hermite, sbz_bessel** out);
+void sbz_bessel_destroy(sbz_bessel* jl);
+/* Interpolated j_l(x) from the cache for cache index il at n points (angular.jl:29-48). */
+int sbz_bessel_eval(const sbz_bessel* jl, int il, int n, const double* x, double* out);
+
+/* los_integrate(Ss, ls, τs, ks, jl; l_limber) (src/observables/angular.jl:109-185).
+ * S[(it*nk + ik)*nsrc + s] -> out[(ik*nl + il)*nsrc + s]; l_limber applies to every source. */
+int sbz_los_integrate(const sbz_bessel* jl, int nsrc, const double* S, int ntau, const double* taus,
+                      int nk, const double* ks, int l_limber, double* out);
+int sbz_los_integrate_device(const sbz_bessel* jl, int nsrc, const double* S, int ntau, const double* taus,
+                             int nk, const double* ks, int l_limber, double* out, void* stream);
+
+/* spectrum_cmb(ΘlAs, ΘlBs, P0s, ls, ks) (src/observables/angular.jl:198-223): natural cubic
+ * spline through (0,0) and (k, 2/π k² P0 Θ_A Θ_B), integrated exactly.  Th[ik*nl + il]. */
+int sbz_cl_integrate(int nk, const double* ks, const double* P0, int nl, const double* ThA,
+                     const double* ThB, double* Cl);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

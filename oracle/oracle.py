@@ -301,7 +301,7 @@ def spectrum_matter(bg: Background, ks, kτini=1e-2, τinimax=1e-4):
 
 
 def spectrum_cmb(bg: Background, modes, jl: BesselCache, ls_out=None, *, kinterp=None, dkt0=np.pi,
-                 xs=None, taucut=1e-2, l_limber=10, normalization="Dl", return_parts=False):
+                 xs=None, taucut=1e-2, l_limber=10, normalization="Dl", return_parts=False, taus=None):
     """Angular spectra C_l/D_l for modes like ['TT','EE','ψψ'] (src/observables/angular.jl:260-359)."""
     modes = list(modes)
     joined = "".join(modes)
@@ -315,9 +315,11 @@ def spectrum_cmb(bg: Background, modes, jl: BesselCache, ls_out=None, *, kinterp
     tau0 = bg.tau0
     kmin, kmax = kinterp.xs[-1], kinterp.xs[0]
     ks_fine = lingrid(kmin, kmax, step=dkt0 / tau0)
-    taus = bg.t[bg.t >= taucut]
-    xs = cosgrid(0.0, 1.0, length=300) if xs is None else np.asarray(xs)
-    taus = taus[0] + (taus[-1] - taus[0]) * xs
+    if taus is None:
+        taus = bg.t[bg.t >= taucut]
+        xs = cosgrid(0.0, 1.0, length=300) if xs is None else np.asarray(xs)
+        taus = taus[0] + (taus[-1] - taus[0]) * xs
+    taus = np.asarray(taus, dtype=np.float64)
     # coarse solve (ptivini = -Inf -> background start) and k-interpolation
     Sc, status, stats = bg.solve_pt(kinterp.xs, bg.t[0], taus, mode=0)  # [ik, it, 3]
     M = kinterp.matrix(ks_fine)  # [nfine, ncoarse]

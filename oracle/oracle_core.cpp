@@ -578,8 +578,10 @@ extern "C" orc_bg* orc_bg_solve(const orc_params* p, const orc_model* m, const o
   {
     const int nk = (int)B->knots.size();
     std::vector<double> d(3 * nk);
+    // stencils exclude knot 0: the initial condition dT = 0 is off quasi-equilibrium and the first
+    // knots resolve a ~1e-14-wide transient that must not leak into the slopes
     for (int i = 0; i < nk; ++i) {
-      int lo = std::max(0, std::min(i - 2, nk - 5)), hi = std::min(nk - 1, lo + 4);
+      int lo = std::max(1, std::min(i - 2, nk - 5)), hi = std::min(nk - 1, lo + 4);
       const double xi = B->knots[i].t;
       for (int c = 0; c < 3; ++c) d[3 * i + c] = 0;
       for (int j = lo; j <= hi; ++j) {

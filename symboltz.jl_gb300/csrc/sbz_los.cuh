@@ -1,0 +1,23 @@
+// Launch interface of the line-of-sight kernels (sbz_los.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace sbz {
+
+struct BesselDev {
+  double* y;    // [ix * nl + il]
+  double* dy;   // same layout, or nullptr for linear interpolation
+  int nl, nx;   // nx includes the duplicated last point
+  double xmax, step, invdx, dx;
+  int hermite;
+};
+
+int bessel_build(BesselDev& J, const int* d_ls, int Lmax, cudaStream_t st);
+int bessel_eval(const BesselDev& J, int il, int n, const double* d_x, double* d_out, cudaStream_t st);
+int los_launch(const BesselDev& J, const int* d_ls, int nsrc, const double* d_S, const double* d_taus,
+               const double* d_chi, const double* d_w, int ntau, int nk, const double* d_ks, int il_limber,
+               double* d_out, cudaStream_t st);
+int cl_launch(int nk, const double* d_ks, const double* d_P0, int nl, const double* d_ThA, const double* d_ThB,
+              const double* d_cprime, const double* d_invden, double* d_zbuf, double* d_Cl, cudaStream_t st);
+
+}  // namespace sbz

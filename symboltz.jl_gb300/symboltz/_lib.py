@@ -1,0 +1,108 @@
+"""ctypes binding of libsymboltz_gb300.so (include/symboltz_gb300.h).
+
+The library is the product path: there is no CPU fallback.  Loading fails loudly when the shared
+library has not been built, and compute entry points fail loudly when no CUDA device is present.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "lib", "libsymboltz_gb300.so")
+
+SBZ_OK, SBZ_MAXITERS, SBZ_DTMIN, SBZ_NONFINITE = 0, 1, 2, 3
+SBZ_FP64, SBZ_MIXED = 0, 1
+SBZ_OUT_SOURCES, SBZ_OUT_DELTA_M, SBZ_OUT_STATE = 0, 1, 2
+
+EXPORTS = (
+    "sbz_default_opts", "sbz_last_error", "sbz_momentum_quadrature", "sbz_problem_create", "sbz_problem_destroy",
+    "sbz_problem_nstate", "sbz_solve_bg", "sbz_bg_knots", "sbz_bg_eval", "sbz_bg_coefficients", "sbz_solve_pt", "sbz_solve_pt_device", "sbz_pt_rhs",
+    "sbz_spectrum_matter", "sbz_spectrum_primordial", "sbz_bessel_create", "sbz_bessel_destroy", "sbz_bessel_eval",
+    "sbz_los_integrate", "sbz_los_integrate_device", "sbz_cl_integrate",
+)
+
+
+class Params(C.Structure):
+    _fields_ = [(n, C.c_double) for n in
+                ("h", "Omega_c", "Omega_b", "T0", "Neff", "YHe", "ln_As1e10", "ns", "m_nu_eV", "N_nu")]
+
+
+class Model(C.Structure):
+    _fields_ = [(n, C.c_int) for n in
+                ("lmax_gamma", "lmax_nu", "lmax_h", "nx_h", "Hswitch", "Heswitch", "reionization")]
+
+
+class Opts(C.Structure):
+    _fields_ = [("bg_rtol", C.c_double), ("bg_atol", C.c_double), ("pt_rtol", C.c_double), ("pt_atol", C.c_double),
+                ("tau_ini", C.c_double), ("tau_max", C.c_double), ("maxiters", C.c_int64), ("precision", C.c_int),
+                ("refine_iters", C.c_int), ("table_points", C.c_int), ("warps_per_block", C.c_int)]
+
+
+class SbzError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise SbzError(f"{LIB_PATH} is missing: build it with __graft_entry__.build() (no CPU fallback exists)")
+    L = C.CDLL(LIB_PATH)
+    dp, ip, i64p, vp = C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_int64), C.c_void_p
+    L.sbz_default_opts.argtypes = [C.POINTER(Opts)]
+    L.sbz_default_opts.restype = None
+    L.sbz_last_error.restype = C.c_char_p
+    L.sbz_momentum_quadrature.argtypes = [C.c_int, dp, dp]
+    L.sbz_problem_create.argtypes = [C.POINTER(Model), C.POINTER(Params), C.c_int, C.POINTER(Opts), C.POINTER(vp)]
+    L.sbz_problem_destroy.argtypes = [vp]
+    L.sbz_problem_destroy.restype = None
+    L.sbz_problem_nstate.argtypes = [vp]
+    L.sbz_solve_bg.argtypes = [vp, dp, dp, dp, ip]
+    L.sbz_bg_knots.argtypes = [vp, C.c_int, C.c_int, dp, dp]
+    L.sbz_bg_eval.argtypes = [vp, C.c_int, C.c_int, dp, dp]
+    L.sbz_bg_coefficients.argtypes = [vp, C.c_int, C.c_int, dp, dp]
+    L.sbz_solve_pt.argtypes = [vp, C.c_int, ip, dp, dp, C.c_int, dp, C.c_int, dp, ip, i64p]
+    L.sbz_solve_pt_device.argtypes = [vp, C.c_int, vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp]
+    L.sbz_pt_rhs.argtypes = [vp, C.c_int, ip, dp, dp, dp, dp, dp]
+    L.sbz_spectrum_matter.argtypes = [vp, C.c_int, ip, dp, C.c_double, C.c_double, dp, ip]
+    L.sbz_spectrum_primordial.argtypes = [vp, C.c_int, C.c_int, dp, dp]
+    L.sbz_bessel_create.argtypes = [C.c_int, ip, C.c_double, C.c_double, C.c_int, C.POINTER(vp)]
+    L.sbz_bessel_destroy.argtypes = [vp]
+    L.sbz_bessel_destroy.restype = None
+    L.sbz_bessel_eval.argtypes = [vp, C.c_int, C.c_int, dp, dp]
+    L.sbz_los_integrate.argtypes = [vp, C.c_int, dp, C.c_int, dp, C.c_int, dp, C.c_int, dp]
+    L.sbz_los_integrate_device.argtypes = [vp, C.c_int, vp, C.c_int, vp, C.c_int, vp, C.c_int, vp, vp]
+    L.sbz_cl_integrate.argtypes = [C.c_int, dp, dp, C.c_int, dp, dp, dp]
+    _lib = L
+    return L
+
+
+def check(code, what=""):
+    if code < 0:
+        raise SbzError(f"{what}: {lib().sbz_last_error().decode()} (code {code})")
+    return code
+
+
+def dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def iptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def i64ptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int64))
+
+
+def f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)

@@ -1,0 +1,176 @@
+"""GPU parity: the CUDA path (through the C-ABI) against the CPU oracle and the reference's fixtures.
+
+Tolerances: the GPU and the oracle integrate the same equations with the same Rodas4 tableau and
+tolerances; they differ in the linear algebra (structured elimination vs dense LU), in FP32
+factorisation with FP64 refinement (mixed precision) and in how background coefficients are
+interpolated, so step sequences differ at the tolerance level.  Parity bar: 1e-4 relative on P(k)
+and on C_l (pt rtol 1e-5), as the reference's matched-tolerance target; bit-level agreement is
+expected for the purely algebraic kernels (Bessel cache, line-of-sight sums, C_l spline integral).
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+import oracle as O  # noqa: E402
+
+MODEL5 = dict(lmax_g=5, lmax_nu=5, lmax_h=5, nx=4, Hswitch=1, Heswitch=6, reionization=1)
+
+
+@pytest.fixture(scope="module")
+def S():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    import symboltz
+    return symboltz
+
+
+@pytest.fixture(scope="module")
+def bg5():
+    return O.Background(O.PLANCK18, MODEL5)
+
+
+@pytest.fixture(scope="module", params=["mixed", "fp64"])
+def prob5(S, request):
+    M = S.ΛCDM(lmax=5)
+    p = S.CosmologyProblem(M, S.parameters_Planck18(M), precision=request.param)
+    p.solvebg()
+    return p
+
+
+def test_background_matches_oracle(S, prob5, bg5):
+    bg = prob5.solvebg()
+    assert bg.status[0] == 0
+    assert abs(bg.tau0[0] / bg5.tau0 - 1) < 1e-8
+    assert abs(bg.kappa0[0] / bg5.kappa0 - 1) < 1e-8
+    assert abs(bg.taurec[0] / bg5.taurec - 1) < 1e-5
+
+
+def test_pk_matches_oracle(S, prob5, bg5, golden):
+    d = np.loadtxt(os.path.join(golden, "class_Pk.txt"))
+    ks = d[:, 0]
+    P, st = S.spectrum_matter(prob5, ks, return_status=True)
+    Po, sto, _ = O.spectrum_matter(bg5, ks)
+    assert np.all(st == 0) and np.all(sto == 0)
+    rel = np.abs(P / Po - 1)
+    assert np.max(rel[ks > 0.15]) < 1e-4, np.max(rel)
+    assert np.linalg.norm(P - Po) <= 1e-4 * np.linalg.norm(Po)
+    # and against the reference's CLASS fixture at its own tolerance (test/runtests.jl:871-876)
+    assert np.linalg.norm(P - d[:, 1]) <= 1e-3 * np.linalg.norm(d[:, 1])
+
+
+@pytest.mark.parametrize("tol,bar", [(1e-5, 1e-3), (1e-7, 2e-5)])
+def test_sources_match_oracle(S, prob5, tol, bar):
+    """Line-of-sight sources; differences are at the integrator-tolerance level and shrink with it."""
+    M = S.ΛCDM(lmax=5)
+    prob = S.CosmologyProblem(M, S.parameters_Planck18(M), pt_rtol=tol, pt_atol=tol,
+                              precision="fp64" if prob5.opts.precision == 0 else "mixed")
+    bgo = O.Background(O.PLANCK18, MODEL5, pt_rtol=tol, pt_atol=tol)
+    ks = np.array([2.0, 50.0, 300.0, 2000.0])
+    taus = np.linspace(bgo.tau0 * 0.01, bgo.tau0 * 0.999, 64)
+    out, st, _ = S.solvept(prob, ks, 1e-6, saveat=taus, output="sources")
+    ref, sto, _ = bgo.solve_pt(ks, 1e-6, taus, mode=0)
+    assert np.all(st == 0) and np.all(sto == 0)
+    for s in range(3):
+        scale = np.max(np.abs(ref[:, :, s]), axis=1, keepdims=True) + 1e-300
+        assert np.max(np.abs(out[:, :, s] - ref[:, :, s]) / scale) < bar, s
+
+
+def test_state_matches_oracle(S, prob5):
+    tol = 1e-7
+    M = S.ΛCDM(lmax=5)
+    prob = S.CosmologyProblem(M, S.parameters_Planck18(M), pt_rtol=tol, pt_atol=tol,
+                              precision="fp64" if prob5.opts.precision == 0 else "mixed")
+    bgo = O.Background(O.PLANCK18, MODEL5, pt_rtol=tol, pt_atol=tol)
+    ks = np.array([0.5, 30.0, 800.0])
+    taus = np.array([1e-6, 1e-3, 0.02, 0.06, 0.5, bgo.tau0 * (1 - 1e-6)])
+    out, st, _ = S.solvept(prob, ks, 1e-6, saveat=taus, output="state")
+    ref, sto, _ = bgo.solve_pt(ks, 1e-6, taus, mode=2)
+    assert np.all(st == 0) and np.all(sto == 0)
+    g = out[:, :, S.state_index(M)]
+    np.testing.assert_allclose(g[:, 0], ref[:, 0], rtol=1e-12, atol=1e-300)  # initial conditions
+    # per component, in units of the integrator's error weights (atol + rtol |y|)
+    w = tol + tol * np.max(np.abs(ref), axis=1, keepdims=True)
+    assert np.max(np.abs(g - ref) / w) < 50
+
+
+def test_failed_modes_report_status(S, prob5):
+    P, st = S.spectrum_matter(prob5, np.array([0.0, np.nan, 1.0]), return_status=True)
+    assert st[0] != 0 and st[1] != 0 and st[2] == 0
+
+
+def test_maxiters_status(S):
+    M = S.ΛCDM(lmax=5)
+    p = S.CosmologyProblem(M, S.parameters_Planck18(M), maxiters=20)
+    P, st = S.spectrum_matter(p, np.array([1.0, 100.0]), return_status=True)
+    assert np.all(st == 1)
+
+
+def test_bessel_cache_matches_oracle(S):
+    from scipy.special import spherical_jn
+    ls = np.array([2, 3, 10, 57, 200, 999, 1500])
+    jl = S.SphericalBesselCache(ls)
+    jo = O.BesselCache(ls)
+    xs = np.concatenate([[0.0], np.geomspace(1e-3, jl.xmax * 0.999, 4000)])
+    for il in range(len(ls)):
+        a, b = jl(il, xs), jo(il, xs)
+        np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-14)
+        np.testing.assert_allclose(a, spherical_jn(ls[il], xs), atol=1e-5)
+
+
+def test_los_and_cl_match_oracle(S):
+    rng = np.random.default_rng(0)
+    ls = np.array([2, 5, 10, 30, 100, 400])
+    jl, jo = S.SphericalBesselCache(ls), O.BesselCache(ls)
+    taus = np.sort(rng.uniform(0.05, 3.0, 200))
+    ks = np.linspace(1.0, 150.0, 97)
+    Sg = rng.standard_normal((len(taus), len(ks), 3))
+    for l_limber in (2**31 - 1, 10):
+        a = S.los_integrate(Sg, ls, taus, ks, jl, l_limber=l_limber)
+        b = O.los_integrate(Sg, taus, ks, jo, l_limber)
+        np.testing.assert_allclose(a, b, rtol=1e-10, atol=1e-12 * np.max(np.abs(b)))
+    P0 = rng.uniform(0.5, 1.5, len(ks))
+    ThA, ThB = rng.standard_normal((len(ks), len(ls))), rng.standard_normal((len(ks), len(ls)))
+    np.testing.assert_allclose(S.spectrum_cmb(ThA, ThB, P0, ls, ks), O.cl_integrate(ks, P0, ThA, ThB), rtol=1e-11)
+
+
+def test_cmb_matches_oracle_and_class(S, golden, bg5):
+    d = np.loadtxt(os.path.join(golden, "class_Cl.txt"))
+    lc = d[:, 0]
+    ls = np.unique(np.round(np.exp(np.linspace(np.log(lc[0]), np.log(lc[-1]), 200))).astype(int))
+    M = S.ΛCDM(lmax=5)
+    prob = S.CosmologyProblem(M, S.parameters_Planck18(M))
+    jl = S.SphericalBesselCache(ls)
+    Dl = S.spectrum_cmb(["TT", "EE", "ψψ"], prob, jl, lc, normalization="Dl")
+    # the reference's default τ-grid starts at the first background knot >= τcut; the two background
+    # integrations place knots slightly differently, so parity is measured on one shared grid
+    t = bg5.t[bg5.t >= 1e-2]
+    taus = t[0] + (bg5.tau0 * (1 - 1e-12) - t[0]) * S.cosgrid(0.0, 1.0, length=300)
+    Dg = S.spectrum_cmb(["TT", "EE", "ψψ"], prob, jl, lc, normalization="Dl", taus=taus)
+    Do = O.spectrum_cmb(bg5, ["TT", "EE", "ψψ"], O.BesselCache(ls), lc, taus=taus)
+    for j in range(3):
+        assert np.linalg.norm(Dg[:, j] - Do[:, j]) <= 1e-4 * np.linalg.norm(Do[:, j]), j
+        assert np.linalg.norm(Dl[:, j] - d[:, j + 1]) <= 2e-3 * np.linalg.norm(d[:, j + 1]), j
+
+
+def test_rhs_matches_oracle(S, prob5, bg5):
+    """The GPU operator (f = J y, ∂f/∂τ) against the oracle's dense right-hand side."""
+    rng = np.random.default_rng(1)
+    M = S.ΛCDM(lmax=5)
+    idx = S.state_index(M)
+    ks = np.array([0.3, 3.0, 30.0, 300.0, 3000.0])
+    taus = np.array([1e-6 * 1.7, 3e-5, 2e-3, 0.06, 1.5])
+    for tau in taus:
+        Yo = rng.standard_normal((len(ks), bg5.nstate))
+        Yg = np.zeros_like(Yo)
+        Yg[:, idx] = Yo
+        f, ft = S.pt_rhs(prob5, ks, np.full(len(ks), tau), Yg)
+        for i, k in enumerate(ks):
+            fo, Jo, fto = bg5.rhs(k, tau, Yo[i], jac=True)
+            scale = np.abs(Jo) @ np.abs(Yo[i]) + 1e-300
+            np.testing.assert_array_less(np.abs(f[i, idx] - fo) / scale, 1e-6, err_msg=f"f tau={tau} k={k}")
+            tscale = np.abs(fto).max() + 1e-300
+            assert np.max(np.abs(ft[i, idx] - fto)) / tscale < 1e-3, (tau, k)

@@ -1,0 +1,111 @@
+"""CPU-side checks of the C-ABI library: it loads and exports every entry point that
+include/symboltz_gb300.h declares (no compute calls: there is no GPU here), plus host logic."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "symboltz_gb300.h")
+
+
+def declared_symbols():
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(sbz_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_header_and_binding_agree():
+    from symboltz import _lib
+    assert sorted(_lib.EXPORTS) == declared_symbols()
+
+
+def test_library_exports_every_declared_symbol():
+    from symboltz import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("library not built")
+    L = _lib.lib()
+    for name in declared_symbols():
+        assert hasattr(L, name), name
+
+
+def test_default_options():
+    import ctypes as C
+    from symboltz import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("library not built")
+    o = _lib.Opts()
+    _lib.lib().sbz_default_opts(C.byref(o))
+    assert o.bg_rtol == 1e-7 and o.pt_rtol == 1e-5 and o.tau_ini == 1e-6 and o.maxiters == 100000
+    assert o.precision == _lib.SBZ_MIXED
+
+
+def test_momentum_quadrature_host(golden):
+    """The product's quadrature is host code; it matches the published table without a GPU."""
+    from symboltz import _lib
+    import symboltz as S
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("library not built")
+    tab = np.loadtxt(os.path.join(golden, "quadrature.txt"))
+    for row in tab:
+        N = int(row[0])
+        x, W = S.momentum_quadrature(N)
+        np.testing.assert_allclose(x, row[1:1 + N], atol=6e-6)
+        np.testing.assert_allclose(W, row[9:9 + N], atol=6e-6)
+
+
+def test_host_stages_run_and_gpu_calls_fail_loudly_without_gpu():
+    """Problem set-up and the background stage are host code; perturbation solves need the GPU
+    and raise (no CPU fallback)."""
+    import torch
+    from symboltz import _lib
+    import symboltz as S
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("library not built")
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    p = S.CosmologyProblem(S.ΛCDM(lmax=5), S.parameters_Planck18())
+    assert p.solvebg().status[0] == 0
+    with pytest.raises(S.SbzError):
+        S.spectrum_matter(p, [1.0])
+
+
+def test_background_and_table_match_oracle():
+    """The product's host background (solve, spline, coefficient table) against the oracle."""
+    from symboltz import _lib
+    import symboltz as S
+    import oracle as O
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("library not built")
+    p = S.CosmologyProblem(S.ΛCDM(lmax=5), S.parameters_Planck18())
+    bg = p.solvebg()
+    o = O.Background(O.PLANCK18, dict(lmax_g=5, lmax_nu=5, lmax_h=5, nx=4, Hswitch=1, Heswitch=6, reionization=1))
+    assert abs(bg.tau0[0] / o.tau0 - 1) < 1e-8
+    assert abs(bg.kappa0[0] / o.kappa0 - 1) < 1e-8
+    assert abs(bg.taurec[0] / o.taurec - 1) < 1e-5  # flat maximum of the visibility
+    # from the second table node on: the table smooths the ~1e-14-wide ΔT transient at the initial
+    # time over its first interval
+    ts = np.geomspace(1e-6 * 1.01, o.tau0 * (1 - 1e-9), 400)
+    a, b, c = bg.eval(ts), o.eval(ts), bg.coefficients(ts)
+    # the two background integrations take slightly different steps (rounding), so spline values
+    # agree to ~1e-7 (a, ℋ) and ~1e-6 where Xe changes fast (κ̇, Xe in reionization)
+    for j, tol in ((0, 1e-7), (1, 1e-7), (2, 2e-6), (7, 2e-6)):  # a, ℋ, κ̇, Xe
+        np.testing.assert_allclose(a[:, j], b[:, j], rtol=tol)
+    np.testing.assert_allclose(a[:, 6], b[:, 6], rtol=1e-5)  # c_s² (slope-sensitive ΔT spline)
+    for q, j, tol in ((0, 0, 1e-7), (1, 1, 1e-7), (2, 2, 2e-6)):  # table interpolation as the kernels read it
+        np.testing.assert_allclose(c[:, q], b[:, j], rtol=tol)
+    np.testing.assert_allclose(c[:, 3], b[:, 6], rtol=1e-5)
+
+
+def test_grids_match_reference_definitions():
+    import symboltz as S
+    g = S.cosgrid(0.0, 1.0, length=300)
+    assert g[0] == 0.0 and abs(g[-1] - 1.0) < 1e-15 and np.all(np.diff(g) > 0)
+    lg = S.loggrid(1e-4, 1.0, length=100)
+    assert lg[0] == 1e-4 and lg[-1] == 1.0
+    ci = S.ChebyshevInterpolator(1e-2, 2e3, 60)
+    assert ci.xs[0] == 2e3 and ci.xs[-1] == 1e-2 and len(ci.xs) == 61
+    # barycentric interpolation reproduces low-order polynomials exactly
+    kf = np.linspace(1e-2, 2e3, 1001)
+    Mx = ci.matrix(kf)
+    np.testing.assert_allclose(Mx @ (ci.xs**2), kf**2, rtol=1e-9)
