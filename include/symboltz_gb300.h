@@ -132,6 +132,27 @@ int sbz_los_integrate(const sbz_bessel* jl, int nsrc, const double* S, int ntau,
 int sbz_los_integrate_device(const sbz_bessel* jl, int nsrc, const double* S, int ntau, const double* taus,
                              int nk, const double* ks, int l_limber, double* out, void* stream);
 
+/* k-interpolation of the sources (src/observables/fourier.jl:227-247,464-547) */
+#define SBZ_KINTERP_SPLINE 0       /* natural cubic spline in y = f(k) (CubicSplineInterpolator) */
+#define SBZ_KINTERP_BARYCENTRIC 1  /* barycentric formula with weights w in y = f(k) (ChebyshevInterpolator) */
+
+/* spectrum_cmb(modes, prob, jl) (src/observables/angular.jl:260-341) as one device pipeline with host
+ * inputs and outputs: solve the nc coarse modes of cosmology `cosmo` from the background start
+ * with sources saved at taus (source_grid, fourier.jl:267-291), interpolate them to the fine grid
+ * ks_fine (y-values yc/yf = f(k); weights wc for SBZ_KINTERP_BARYCENTRIC), zero the last time,
+ * line-of-sight integrate over the cache's l (T and E without Limber, ψ with l_limber), scale
+ * Θ_T and Θ_E, and integrate C_l for npair source pairs (0 = T, 1 = E, 2 = ψ):
+ * out_cl[q*nl + il].  status[nc] receives the per-mode solver status (may be NULL). */
+int sbz_spectrum_cmb(sbz_problem* pb, int cosmo, const sbz_bessel* jl, int nc, const double* ks_coarse, const double* yc,
+                     const double* wc, int interp, int ntau, const double* taus, int nf, const double* ks_fine,
+                     const double* yf, int npair, const int* pair_a, const int* pair_b, int l_limber, double* out_cl,
+                     int* status);
+/* Launch everything of this problem on an external CUDA stream (NULL: back to an own stream). */
+int sbz_problem_set_stream(sbz_problem* pb, void* stream);
+/* CUDA-event durations (ms) of the last sbz_spectrum_cmb: H2D, perturbations, k-interpolation,
+ * line of sight, C_l, D2H, total, (reserved). */
+int sbz_problem_timings(const sbz_problem* pb, double* ms8);
+
 /* spectrum_cmb(ΘlAs, ΘlBs, P0s, ls, ks) (src/observables/angular.jl:198-223): natural cubic
  * spline through (0,0) and (k, 2/π k² P0 Θ_A Θ_B), integrated exactly.  Th[ik*nl + il]. */
 int sbz_cl_integrate(int nk, const double* ks, const double* P0, int nl, const double* ThA,

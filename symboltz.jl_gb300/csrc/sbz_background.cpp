@@ -404,6 +404,8 @@ void background_table(Background& B, int ntab) {
   B.dlnt = (std::log(B.tau0) - B.lnt0) / (ntab - 1);
   B.tab.assign((size_t)ntab * kTabStride, 0.0);
   B.tabtau.resize(ntab);
+  // nodes are independent; inside an outer parallel loop over cosmologies this runs serially
+#pragma omp parallel for schedule(static)
   for (int g = 0; g < ntab; ++g) {
     double tau = (g == ntab - 1) ? B.tau0 : (g == 0 ? B.tau_start : std::exp(B.lnt0 + g * B.dlnt));
     B.tabtau[g] = tau;

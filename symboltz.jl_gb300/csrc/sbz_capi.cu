@@ -47,6 +47,34 @@ struct DevBuf {
   template <class T> T* as() const { return static_cast<T*>(p); }
 };
 
+// natural-spline Thomas factors for points X[0..n-1] (interior rows 1..n-2)
+void spline_factors(const std::vector<double>& X, std::vector<double>& cprime, std::vector<double>& invden) {
+  const int n = (int)X.size();
+  cprime.assign(n, 0.0); invden.assign(n, 0.0);
+  for (int i = 1; i <= n - 2; ++i) {
+    const double h0 = X[i] - X[i - 1], h1 = X[i + 1] - X[i];
+    invden[i] = 1.0 / (2 * (h0 + h1) - h0 * (i > 1 ? cprime[i - 1] : 0.0));
+    cprime[i] = h1 * invden[i];
+  }
+}
+
+template <class T>
+cudaError_t up(DevBuf& b, const T* h, size_t n, cudaStream_t st) {
+  cudaError_t e = b.ensure(sizeof(T) * std::max<size_t>(n, 1));
+  if (e != cudaSuccess || n == 0) return e;
+  return cudaMemcpyAsync(b.p, h, sizeof(T) * n, cudaMemcpyHostToDevice, st);
+}
+
+int los_weights(const double* taus, int ntau, std::vector<double>& chi, std::vector<double>& w) {
+  chi.resize(ntau); w.resize(ntau);
+  const double t0 = taus[ntau - 1];
+  for (int i = 0; i < ntau; ++i) chi[i] = t0 - taus[i];
+  w[0] = 0.5 * (taus[1] - taus[0]);
+  for (int i = 1; i < ntau - 1; ++i) w[i] = 0.5 * (taus[i + 1] - taus[i - 1]);
+  w[ntau - 1] = 0.5 * (taus[ntau - 1] - taus[ntau - 2]);
+  return SBZ_OK;
+}
+
 }  // namespace
 
 struct sbz_problem {
@@ -65,8 +93,17 @@ struct sbz_problem {
   cudaStream_t stream = nullptr;
   DevBuf d_model, d_comps, d_cosmos, d_tables, d_counter;
   DevBuf d_k, d_ti, d_cosmo, d_order, d_taus, d_out, d_status, d_steps;
+  DevBuf c_y, c_yf, c_iv, c_cp, c_id, c_z, c_Sf, c_Sp, c_ks, c_ls, c_Th, c_Thp, c_P0, c_cz, c_cl, c_pa, c_pb, c_src, c_M,
+      c_chi, c_w, c_taus, c_kf;
   int64_t table_stride = 0;
+  bool own_stream = true;
+  cudaEvent_t ev[12] = {};
+  double timings[8] = {};
 };
+
+namespace {
+enum { T_H2D = 0, T_PT, T_KINTERP, T_LOS, T_CL, T_D2H, T_TOTAL };
+}
 
 struct sbz_bessel {
   sbz::BesselDev J{};
@@ -121,13 +158,41 @@ static int ensure_device(sbz_problem* pb) {
 
 static int upload_tables(sbz_problem* pb);
 
+static int ensure_events(sbz_problem* pb) {
+  if (pb->ev[0]) return SBZ_OK;
+  for (auto& e : pb->ev) if (cudaEventCreate(&e) != cudaSuccess) return fail(SBZ_ERR_CUDA, "event");
+  return SBZ_OK;
+}
+
+int sbz_problem_set_stream(sbz_problem* pb, void* stream) {
+  if (!pb) return fail(SBZ_ERR_ARG, "null problem");
+  int r = ensure_device(pb);
+  if (r != SBZ_OK) return r;
+  if (pb->own_stream && pb->stream) cudaStreamDestroy(pb->stream);
+  pb->stream = stream ? (cudaStream_t)stream : nullptr;
+  pb->own_stream = false;
+  if (!stream) { pb->own_stream = true; if (cudaStreamCreateWithFlags(&pb->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(SBZ_ERR_CUDA, "stream"); }
+  return SBZ_OK;
+}
+
+int sbz_problem_timings(const sbz_problem* pb, double* ms8) {
+  if (!pb || !ms8) return fail(SBZ_ERR_ARG, "null argument");
+  for (int i = 0; i < 8; ++i) ms8[i] = pb->timings[i];
+  return SBZ_OK;
+}
+
 void sbz_problem_destroy(sbz_problem* pb) {
   if (!pb) return;
   if (pb->stream) cudaStreamSynchronize(pb->stream);
   for (DevBuf* b : {&pb->d_model, &pb->d_comps, &pb->d_cosmos, &pb->d_tables, &pb->d_counter, &pb->d_k, &pb->d_ti,
                     &pb->d_cosmo, &pb->d_order, &pb->d_taus, &pb->d_out, &pb->d_status, &pb->d_steps})
     b->release();
-  if (pb->stream) cudaStreamDestroy(pb->stream);
+  for (DevBuf* b : {&pb->c_y, &pb->c_yf, &pb->c_iv, &pb->c_cp, &pb->c_id, &pb->c_z, &pb->c_Sf, &pb->c_Sp, &pb->c_ks, &pb->c_ls,
+                    &pb->c_Th, &pb->c_Thp, &pb->c_P0, &pb->c_cz, &pb->c_cl, &pb->c_pa, &pb->c_pb, &pb->c_src, &pb->c_M, &pb->c_chi,
+                    &pb->c_w, &pb->c_taus, &pb->c_kf})
+    b->release();
+  for (auto& e : pb->ev) if (e) cudaEventDestroy(e);
+  if (pb->stream && pb->own_stream) cudaStreamDestroy(pb->stream);
   delete pb;
 }
 
@@ -141,7 +206,7 @@ int sbz_solve_bg(sbz_problem* pb, double* tau0, double* kappa0, double* taurec, 
   pb->cds.assign(nc, sbz::CosmoDesc{});
   const int ntab = pb->opts.table_points;
   std::vector<int> cst(nc, SBZ_OK);
-#pragma omp parallel for schedule(dynamic, 1)
+#pragma omp parallel for schedule(dynamic, 1) if (nc > 1)
   for (int c = 0; c < nc; ++c) {
     sbz::Background& B = pb->bgs[c];
     sbz_opts bo = pb->opts;
@@ -363,6 +428,178 @@ int sbz_spectrum_matter(sbz_problem* pb, int nk, const int* cosmo, const double*
   return SBZ_OK;
 }
 
+int sbz_spectrum_cmb(sbz_problem* pb, int cosmo, const sbz_bessel* jl, int nc, const double* ks_coarse, const double* yc,
+                     const double* wc, int interp, int ntau, const double* taus, int nf, const double* ks_fine, const double* yf,
+                     int npair, const int* pair_a, const int* pair_b, int l_limber, double* out_cl, int* status) {
+  if (!pb || !jl || !ks_coarse || !yc || !taus || !ks_fine || !yf || !pair_a || !pair_b || !out_cl) return fail(SBZ_ERR_ARG, "null argument");
+  if (nc < 3 || ntau < 2 || nf < 2 || npair < 1 || cosmo < 0 || cosmo >= pb->ncosmo) return fail(SBZ_ERR_ARG, "bad sizes");
+  if (interp == SBZ_KINTERP_BARYCENTRIC && !wc) return fail(SBZ_ERR_ARG, "barycentric weights required");
+  if (!pb->bg_done) return fail(SBZ_ERR_STATE, "call sbz_solve_bg first");
+  if (pb->bg_status[cosmo] != SBZ_OK) return fail(SBZ_ERR_STATE, "background failed for this cosmology");
+  for (int q = 0; q < npair; ++q) if (pair_a[q] < 0 || pair_a[q] > 2 || pair_b[q] < 0 || pair_b[q] > 2) return fail(SBZ_ERR_ARG, "pair sources must be 0 (T), 1 (E) or 2 (psi)");
+  for (int i = 1; i < nf; ++i) if (!(ks_fine[i] > ks_fine[i - 1] && yf[i] > yf[i - 1])) return fail(SBZ_ERR_ARG, "fine grid must increase");
+  const double tau_span = taus[ntau - 1] - taus[0];
+  if (!(jl->J.xmax >= ks_fine[nf - 1] * tau_span)) return fail(SBZ_ERR_ARG, "Bessel cache xmax < kmax * (τ0 - τ_first)");
+  int r = upload_tables(pb);
+  if (r != SBZ_OK) return r;
+  if ((r = ensure_events(pb)) != SBZ_OK) return r;
+  cudaStream_t st = pb->stream;
+  const int nl = jl->J.nl;
+  // which sources: T/E block (no Limber) and ψ (with Limber), as the reference does
+  bool use[3] = {false, false, false};
+  for (int q = 0; q < npair; ++q) { use[pair_a[q]] = true; use[pair_b[q]] = true; }
+  std::vector<int> srcTE, srcP;
+  int colof[3] = {-1, -1, -1};
+  for (int s = 0; s < 2; ++s) if (use[s]) { colof[s] = (int)srcTE.size(); srcTE.push_back(s); }
+  if (use[2]) { srcP.push_back(2); }
+  const int nTE = (int)srcTE.size();
+  const int ns_all = nTE + (use[2] ? 1 : 0);
+  if (use[2]) colof[2] = nTE;
+  // host-side grid data
+  std::vector<int> iv(nf, 0);
+  std::vector<double> cp, idn, Mw;
+  if (interp == SBZ_KINTERP_SPLINE) {
+    for (int i = 1; i < nc; ++i) if (!(yc[i] > yc[i - 1])) return fail(SBZ_ERR_ARG, "coarse y grid must increase for spline interpolation");
+    std::vector<double> Y(yc, yc + nc);
+    spline_factors(Y, cp, idn);
+    for (int f = 0; f < nf; ++f) {
+      int i = (int)(std::upper_bound(yc, yc + nc, yf[f]) - yc) - 1;
+      iv[f] = std::max(0, std::min(i, nc - 2));
+    }
+  } else {
+    Mw.assign((size_t)nf * nc, 0.0);
+    for (int f = 0; f < nf; ++f) {
+      double den = 0; int exact = -1;
+      for (int c = 0; c < nc; ++c) { const double dy = yf[f] - yc[c]; if (dy == 0) { exact = c; break; } }
+      if (exact >= 0) { Mw[(size_t)f * nc + exact] = 1; continue; }
+      for (int c = 0; c < nc; ++c) { const double t = wc[c] / (yf[f] - yc[c]); Mw[(size_t)f * nc + c] = t; den += t; }
+      for (int c = 0; c < nc; ++c) Mw[(size_t)f * nc + c] /= den;
+    }
+  }
+  std::vector<double> chi(ntau), w(ntau);
+  los_weights(taus, ntau, chi, w);
+  std::vector<double> P0(nf);
+  sbz_spectrum_primordial(pb, cosmo, nf, ks_fine, P0.data());
+  std::vector<double> Xk(nf + 1);
+  Xk[0] = 0; for (int i = 0; i < nf; ++i) Xk[i + 1] = ks_fine[i];
+  std::vector<double> kcp, kid;
+  spline_factors(Xk, kcp, kid);
+  std::vector<int> cos(nc, cosmo), ord(nc);
+  std::vector<double> ti(nc, pb->bgs[cosmo].tau_start);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return ks_coarse[a] > ks_coarse[b]; });
+  int ilim = nl;
+  for (int i = 0; i < nl; ++i) if (jl->ls[i] >= l_limber) { ilim = i; break; }
+  std::vector<int> pa(npair), pbv(npair);
+  for (int q = 0; q < npair; ++q) { pa[q] = colof[pair_a[q]]; pbv[q] = colof[pair_b[q]]; }
+
+  SBZ_CUDA(cudaEventRecord(pb->ev[0], st));
+  // inputs
+  SBZ_CUDA(up(pb->d_k, ks_coarse, nc, st));
+  SBZ_CUDA(up(pb->d_ti, ti.data(), nc, st));
+  SBZ_CUDA(up(pb->d_cosmo, cos.data(), nc, st));
+  SBZ_CUDA(up(pb->d_order, ord.data(), nc, st));
+  SBZ_CUDA(pb->d_taus.ensure(sizeof(double) * (size_t)ntau * pb->ncosmo));
+  SBZ_CUDA(cudaMemcpyAsync(pb->d_taus.as<double>() + (size_t)cosmo * ntau, taus, sizeof(double) * ntau, cudaMemcpyHostToDevice, st));
+  SBZ_CUDA(up(pb->c_y, yc, nc, st));
+  SBZ_CUDA(up(pb->c_yf, yf, nf, st));
+  SBZ_CUDA(up(pb->c_iv, iv.data(), nf, st));
+  SBZ_CUDA(up(pb->c_cp, cp.data(), cp.size(), st));
+  SBZ_CUDA(up(pb->c_id, idn.data(), idn.size(), st));
+  SBZ_CUDA(up(pb->c_M, Mw.data(), Mw.size(), st));
+  SBZ_CUDA(up(pb->c_ks, ks_fine, nf, st));
+  SBZ_CUDA(up(pb->c_chi, chi.data(), ntau, st));
+  SBZ_CUDA(up(pb->c_w, w.data(), ntau, st));
+  SBZ_CUDA(up(pb->c_taus, taus, ntau, st));
+  SBZ_CUDA(up(pb->c_P0, P0.data(), nf, st));
+  SBZ_CUDA(up(pb->c_pa, pa.data(), npair, st));
+  SBZ_CUDA(up(pb->c_pb, pbv.data(), npair, st));
+  std::vector<int> srcAll(srcTE); if (use[2]) srcAll.push_back(2);
+  SBZ_CUDA(up(pb->c_src, srcAll.data(), srcAll.size(), st));
+  SBZ_CUDA(pb->d_out.ensure(sizeof(double) * (size_t)nc * ntau * 3));
+  SBZ_CUDA(pb->d_status.ensure(sizeof(int) * nc));
+  SBZ_CUDA(pb->d_steps.ensure(sizeof(int64_t) * 2 * nc));
+  SBZ_CUDA(cudaEventRecord(pb->ev[1], st));
+  // 1. perturbation modes -> coarse sources
+  {
+    sbz::PtArgs A{};
+    A.model = pb->d_model.as<sbz::ModelDesc>(); A.comps = pb->d_comps.as<sbz::CompDesc>(); A.model_n = pb->M.n;
+    A.cosmos = pb->d_cosmos.as<sbz::CosmoDesc>(); A.tables = pb->d_tables.as<double>(); A.table_stride = pb->table_stride;
+    A.item_cosmo = pb->d_cosmo.as<int>(); A.item_k = pb->d_k.as<double>(); A.item_tau_ini = pb->d_ti.as<double>();
+    A.order = pb->d_order.as<int>(); A.nitems = nc;
+    A.taus = pb->d_taus.as<double>(); A.ntau = ntau; A.output = SBZ_OUT_SOURCES;
+    A.out = pb->d_out.as<double>(); A.status = pb->d_status.as<int>(); A.steps = pb->d_steps.as<int64_t>();
+    A.rtol = pb->opts.pt_rtol; A.atol = pb->opts.pt_atol; A.maxiters = pb->opts.maxiters;
+    A.refine = pb->opts.precision == SBZ_MIXED ? std::max(0, pb->opts.refine_iters) : 0;
+    A.counter = pb->d_counter.as<unsigned>();
+    SBZ_CUDA(cudaMemsetAsync(A.counter, 0, sizeof(unsigned), st));
+    r = sbz::pt_launch(A, pb->opts.precision, pb->opts.warps_per_block, pb->num_sms, st);
+    if (r != SBZ_OK) return fail(r, "perturbation kernel");
+    // the perturbation kernel saves the sources at taus of *this* cosmology: A.taus + cosmo*ntau
+  }
+  SBZ_CUDA(cudaEventRecord(pb->ev[2], st));
+  // 2. interpolate to the fine k-grid; zero the last time (χ = 0, angular.jl:296)
+  SBZ_CUDA(pb->c_Sf.ensure(sizeof(double) * (size_t)ntau * nf * std::max(1, nTE)));
+  SBZ_CUDA(pb->c_Sp.ensure(sizeof(double) * (size_t)ntau * nf));
+  SBZ_CUDA(pb->c_z.ensure(sizeof(double) * (size_t)nc * ntau * std::max(1, ns_all)));
+  auto kinterp = [&](int ns, const int* d_src, double* d_out) -> int {
+    if (interp == SBZ_KINTERP_SPLINE)
+      return sbz::kinterp_spline_launch(nc, ntau, ns, nf, d_src, pb->d_out.as<double>(), pb->c_y.as<double>(), pb->c_yf.as<double>(),
+                                        pb->c_iv.as<int>(), pb->c_cp.as<double>(), pb->c_id.as<double>(), pb->c_z.as<double>(), d_out, st);
+    return sbz::kinterp_bary_launch(nc, ntau, ns, nf, d_src, pb->d_out.as<double>(), pb->c_M.as<double>(), d_out, st);
+  };
+  if (nTE > 0 && kinterp(nTE, pb->c_src.as<int>(), pb->c_Sf.as<double>()) != 0) return fail(SBZ_ERR_CUDA, "k-interpolation");
+  if (use[2] && kinterp(1, pb->c_src.as<int>() + nTE, pb->c_Sp.as<double>()) != 0) return fail(SBZ_ERR_CUDA, "k-interpolation");
+  if (nTE > 0) SBZ_CUDA(cudaMemsetAsync(pb->c_Sf.as<double>() + (size_t)(ntau - 1) * nf * nTE, 0, sizeof(double) * nf * nTE, st));
+  if (use[2]) SBZ_CUDA(cudaMemsetAsync(pb->c_Sp.as<double>() + (size_t)(ntau - 1) * nf, 0, sizeof(double) * nf, st));
+  SBZ_CUDA(cudaEventRecord(pb->ev[3], st));
+  // 3. line-of-sight integrals and Θ scaling; gather T/E/ψ into one interleaved Θ array
+  SBZ_CUDA(pb->c_Th.ensure(sizeof(double) * (size_t)nf * nl * std::max(1, nTE)));
+  SBZ_CUDA(pb->c_Thp.ensure(sizeof(double) * (size_t)nf * nl));
+  if (nTE > 0 && sbz::los_launch(jl->J, const_cast<sbz_bessel*>(jl)->d_ls.as<int>(), nTE, pb->c_Sf.as<double>(), pb->c_taus.as<double>(),
+                                 pb->c_chi.as<double>(), pb->c_w.as<double>(), ntau, nf, pb->c_ks.as<double>(), nl, pb->c_Th.as<double>(), st) != 0)
+    return fail(SBZ_ERR_CUDA, "LOS kernel");
+  if (use[2] && sbz::los_launch(jl->J, const_cast<sbz_bessel*>(jl)->d_ls.as<int>(), 1, pb->c_Sp.as<double>(), pb->c_taus.as<double>(),
+                                pb->c_chi.as<double>(), pb->c_w.as<double>(), ntau, nf, pb->c_ks.as<double>(), ilim, pb->c_Thp.as<double>(), st) != 0)
+    return fail(SBZ_ERR_CUDA, "LOS kernel");
+  if (nTE > 0 && sbz::theta_scale_launch(nf, nl, nTE, pb->c_ks.as<double>(), const_cast<sbz_bessel*>(jl)->d_ls.as<int>(),
+                                         colof[0], colof[1], pb->c_Th.as<double>(), st) != 0)
+    return fail(SBZ_ERR_CUDA, "theta scaling");
+  SBZ_CUDA(cudaEventRecord(pb->ev[4], st));
+  // 4. C_l for every requested pair (ψ pairs use the separate Θ_ψ array through an interleave copy)
+  double* dTh = pb->c_Th.as<double>();
+  int nsTh = nTE;
+  if (use[2]) {  // interleave Θ_ψ as the last column
+    SBZ_CUDA(pb->c_cl.ensure(sizeof(double) * (size_t)nf * nl * ns_all));
+    SBZ_CUDA(cudaMemcpy2DAsync(pb->c_cl.p, sizeof(double) * ns_all, dTh, sizeof(double) * std::max(1, nTE), sizeof(double) * nTE,
+                               (size_t)nf * nl, cudaMemcpyDeviceToDevice, st));
+    SBZ_CUDA(cudaMemcpy2DAsync(pb->c_cl.as<double>() + nTE, sizeof(double) * ns_all, pb->c_Thp.p, sizeof(double), sizeof(double),
+                               (size_t)nf * nl, cudaMemcpyDeviceToDevice, st));
+    dTh = pb->c_cl.as<double>();
+    nsTh = ns_all;
+  }
+  DevBuf& kfac = pb->c_kf;  // C_l spline factors
+  SBZ_CUDA(kfac.ensure(sizeof(double) * 2 * (nf + 1)));
+  SBZ_CUDA(cudaMemcpyAsync(kfac.as<double>(), kcp.data(), sizeof(double) * (nf + 1), cudaMemcpyHostToDevice, st));
+  SBZ_CUDA(cudaMemcpyAsync(kfac.as<double>() + (nf + 1), kid.data(), sizeof(double) * (nf + 1), cudaMemcpyHostToDevice, st));
+  SBZ_CUDA(pb->c_cz.ensure(sizeof(double) * (size_t)(nf + 1) * nl * npair + sizeof(double) * (size_t)nl * npair));
+  double* dCl = pb->c_cz.as<double>() + (size_t)(nf + 1) * nl * npair;
+  if (sbz::cl_pairs_launch(nf, pb->c_ks.as<double>(), pb->c_P0.as<double>(), nl, nsTh, dTh, npair, pb->c_pa.as<int>(), pb->c_pb.as<int>(),
+                           kfac.as<double>(), kfac.as<double>() + (nf + 1), pb->c_cz.as<double>(), dCl, st) != 0)
+    return fail(SBZ_ERR_CUDA, "C_l kernel");
+  SBZ_CUDA(cudaEventRecord(pb->ev[5], st));
+  SBZ_CUDA(cudaMemcpyAsync(out_cl, dCl, sizeof(double) * nl * npair, cudaMemcpyDeviceToHost, st));
+  if (status) SBZ_CUDA(cudaMemcpyAsync(status, pb->d_status.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, st));
+  SBZ_CUDA(cudaEventRecord(pb->ev[6], st));
+  SBZ_CUDA(cudaStreamSynchronize(st));
+  float ms;
+  const int map[6][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 4}, {4, 5}, {5, 6}};
+  const int slot[6] = {T_H2D, T_PT, T_KINTERP, T_LOS, T_CL, T_D2H};
+  for (int i = 0; i < 6; ++i) { cudaEventElapsedTime(&ms, pb->ev[map[i][0]], pb->ev[map[i][1]]); pb->timings[slot[i]] = ms; }
+  cudaEventElapsedTime(&ms, pb->ev[0], pb->ev[6]); pb->timings[T_TOTAL] = ms;
+  return SBZ_OK;
+}
+
 // ---------------------------------------------------------------------------------------------
 int sbz_bessel_create(int nl, const int* ls, double xmax, double dx, int hermite, sbz_bessel** out) {
   if (!ls || nl < 1 || !out || !(xmax > 0) || !(dx > 0)) return fail(SBZ_ERR_ARG, "sbz_bessel_create: bad arguments");
@@ -407,15 +644,6 @@ int sbz_bessel_eval(const sbz_bessel* c, int il, int n, const double* x, double*
   return SBZ_OK;
 }
 
-static int los_weights(const double* taus, int ntau, std::vector<double>& chi, std::vector<double>& w) {
-  chi.resize(ntau); w.resize(ntau);
-  const double t0 = taus[ntau - 1];
-  for (int i = 0; i < ntau; ++i) chi[i] = t0 - taus[i];
-  w[0] = 0.5 * (taus[1] - taus[0]);
-  for (int i = 1; i < ntau - 1; ++i) w[i] = 0.5 * (taus[i + 1] - taus[i - 1]);
-  w[ntau - 1] = 0.5 * (taus[ntau - 1] - taus[ntau - 2]);
-  return SBZ_OK;
-}
 
 static int il_limber_of(const sbz_bessel* c, int l_limber) {
   int il = c->J.nl;

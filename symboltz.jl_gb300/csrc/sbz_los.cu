@@ -194,7 +194,144 @@ __global__ void cl_kernel(int nk, const double* __restrict__ ks, const double* _
   Cl[il] = sum;
 }
 
+// ---- source k-interpolation (src/observables/fourier.jl:227-247, 464-547) --------------------
+// Coarse sources Sc[(i*ntau + j)*3 + src[s]] (perturbation-kernel layout) -> fine
+// Sf[(j*nf + f)*ns + s] (line-of-sight layout).  Columns c = j*ns + s.
+// Natural cubic spline in y = f(k): the tridiagonal factors depend only on the coarse y grid.
+__global__ void kinterp_spline_z(int nc, int ntau, int ns, const int* __restrict__ src, const double* __restrict__ Sc,
+                                 const double* __restrict__ y, const double* __restrict__ cprime,
+                                 const double* __restrict__ invden, double* __restrict__ z) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ntau * ns) return;
+  const int j = col / ns, s = src[col % ns];
+  const int ncol = ntau * ns;
+  auto V = [&](int i) { return Sc[((size_t)i * ntau + j) * 3 + s]; };
+  double vprev = V(0), vcur = V(1), dprev = 0;
+  z[col] = 0;
+  for (int i = 1; i <= nc - 2; ++i) {
+    const double vnext = V(i + 1);
+    const double h0 = y[i] - y[i - 1], h1 = y[i + 1] - y[i];
+    const double d = (6 * ((vnext - vcur) / h1 - (vcur - vprev) / h0) - h0 * dprev) * invden[i];
+    z[(size_t)i * ncol + col] = d;
+    dprev = d; vprev = vcur; vcur = vnext;
+  }
+  double znext = 0;
+  z[(size_t)(nc - 1) * ncol + col] = 0;
+  for (int i = nc - 2; i >= 1; --i) {
+    const double zi = z[(size_t)i * ncol + col] - cprime[i] * znext;
+    z[(size_t)i * ncol + col] = zi;
+    znext = zi;
+  }
+}
+
+__global__ void kinterp_spline_eval(int nc, int ntau, int ns, int nf, const int* __restrict__ src, const double* __restrict__ Sc,
+                                    const double* __restrict__ y, const double* __restrict__ yf, const int* __restrict__ iv,
+                                    const double* __restrict__ z, double* __restrict__ Sf) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t total = (size_t)ntau * nf * ns;
+  if (t >= total) return;
+  const int s = (int)(t % ns), f = (int)((t / ns) % nf), j = (int)(t / ((size_t)ns * nf));
+  const int ncol = ntau * ns, col = j * ns + s;
+  const int i = iv[f];
+  const double h = y[i + 1] - y[i], a = y[i + 1] - yf[f], b = yf[f] - y[i];
+  const double v0 = Sc[((size_t)i * ntau + j) * 3 + src[s]], v1 = Sc[((size_t)(i + 1) * ntau + j) * 3 + src[s]];
+  const double z0 = z[(size_t)i * ncol + col], z1 = z[(size_t)(i + 1) * ncol + col];
+  Sf[t] = z0 * a * a * a / (6 * h) + z1 * b * b * b / (6 * h) + (v1 / h - z1 * h / 6) * b + (v0 / h - z0 * h / 6) * a;
+}
+
+// Barycentric interpolation (Chebyshev points): Sf = Σ_c M[f][c] Sc[c], M built on the host.
+__global__ void kinterp_bary(int nc, int ntau, int ns, int nf, const int* __restrict__ src, const double* __restrict__ Sc,
+                             const double* __restrict__ Mw, double* __restrict__ Sf) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t total = (size_t)ntau * nf * ns;
+  if (t >= total) return;
+  const int s = (int)(t % ns), f = (int)((t / ns) % nf), j = (int)(t / ((size_t)ns * nf));
+  const double* m = Mw + (size_t)f * nc;
+  double acc = 0;
+  for (int c = 0; c < nc; ++c) acc = fma(m[c], Sc[((size_t)c * ntau + j) * 3 + src[s]], acc);
+  Sf[t] = acc;
+}
+
+// Θ scaling after the line-of-sight integral (angular.jl:301-306): T /= k; E *= √((l+2)!/(l-2)!)/k².
+__global__ void theta_scale(int nk, int nl, int ns, const double* __restrict__ ks, const int* __restrict__ ls,
+                            int sT, int sE, double* __restrict__ Th) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)nk * nl) return;
+  const int ik = (int)(t / nl), il = (int)(t % nl);
+  const double k = ks[ik], l = ls[il];
+  if (sT >= 0) Th[t * ns + sT] /= k;
+  if (sE >= 0) Th[t * ns + sE] *= sqrt((l + 2) * (l + 1) * l * (l - 1)) / (k * k);
+}
+
+// C_l from interleaved Θ [(ik*nl + il)*ns + s] for pairs (a, b): same spline integral as cl_kernel.
+__global__ void cl_pairs_kernel(int nk, const double* __restrict__ ks, const double* __restrict__ P0, int nl, int ns,
+                                const double* __restrict__ Th, int npair, const int* __restrict__ pa, const int* __restrict__ pb,
+                                const double* __restrict__ cprime, const double* __restrict__ invden,
+                                double* __restrict__ zbuf, double* __restrict__ Cl) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nl * npair) return;
+  const int il = t % nl, q = t / nl;
+  const int A = pa[q], Bq = pb[q];
+  const int np = nk + 1;
+  const int stride = nl * npair;
+  auto X = [&](int i) { return i == 0 ? 0.0 : ks[i - 1]; };
+  auto Y = [&](int i) {
+    if (i == 0) return 0.0;
+    const size_t o = ((size_t)(i - 1) * nl + il) * ns;
+    return (2.0 / M_PI) * ks[i - 1] * ks[i - 1] * P0[i - 1] * Th[o + A] * Th[o + Bq];
+  };
+  double* z = zbuf + t;
+  double yprev = Y(0), ycur = Y(1), dprev = 0;
+  for (int i = 1; i <= np - 2; ++i) {
+    const double ynext = Y(i + 1);
+    const double h0 = X(i) - X(i - 1), h1 = X(i + 1) - X(i);
+    const double d = (6 * ((ynext - ycur) / h1 - (ycur - yprev) / h0) - h0 * dprev) * invden[i];
+    z[(size_t)i * stride] = d;
+    dprev = d; yprev = ycur; ycur = ynext;
+  }
+  double znext = 0, sum = 0, ynext = Y(np - 1);
+  for (int i = np - 2; i >= 0; --i) {
+    const double zi = (i >= 1) ? z[(size_t)i * stride] - cprime[i] * znext : 0.0;
+    const double yi = Y(i);
+    const double h = X(i + 1) - X(i);
+    sum += h * (yi + ynext) * 0.5 - h * h * h * (zi + znext) / 24.0;
+    znext = zi; ynext = yi;
+  }
+  Cl[t] = sum;
+}
+
 }  // namespace
+
+int kinterp_spline_launch(int nc, int ntau, int ns, int nf, const int* d_src, const double* d_Sc, const double* d_y,
+                          const double* d_yf, const int* d_iv, const double* d_cprime, const double* d_invden, double* d_z,
+                          double* d_Sf, cudaStream_t st) {
+  const int ncol = ntau * ns;
+  kinterp_spline_z<<<(ncol + 127) / 128, 128, 0, st>>>(nc, ntau, ns, d_src, d_Sc, d_y, d_cprime, d_invden, d_z);
+  const size_t total = (size_t)ntau * nf * ns;
+  kinterp_spline_eval<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(nc, ntau, ns, nf, d_src, d_Sc, d_y, d_yf, d_iv, d_z, d_Sf);
+  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+int kinterp_bary_launch(int nc, int ntau, int ns, int nf, const int* d_src, const double* d_Sc, const double* d_M, double* d_Sf,
+                        cudaStream_t st) {
+  const size_t total = (size_t)ntau * nf * ns;
+  kinterp_bary<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(nc, ntau, ns, nf, d_src, d_Sc, d_M, d_Sf);
+  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+int theta_scale_launch(int nk, int nl, int ns, const double* d_ks, const int* d_ls, int sT, int sE, double* d_Th, cudaStream_t st) {
+  const size_t total = (size_t)nk * nl;
+  theta_scale<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(nk, nl, ns, d_ks, d_ls, sT, sE, d_Th);
+  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+int cl_pairs_launch(int nk, const double* d_ks, const double* d_P0, int nl, int ns, const double* d_Th, int npair,
+                    const int* d_pa, const int* d_pb, const double* d_cprime, const double* d_invden, double* d_z, double* d_Cl,
+                    cudaStream_t st) {
+  const int total = nl * npair;
+  cl_pairs_kernel<<<(total + 127) / 128, 128, 0, st>>>(nk, d_ks, d_P0, nl, ns, d_Th, npair, d_pa, d_pb, d_cprime, d_invden, d_z, d_Cl);
+  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
 
 int bessel_build(BesselDev& J, const int* d_ls, int Lmax, cudaStream_t st) {
   const int N = J.nx - 1;

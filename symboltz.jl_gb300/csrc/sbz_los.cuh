@@ -20,4 +20,14 @@ int los_launch(const BesselDev& J, const int* d_ls, int nsrc, const double* d_S,
 int cl_launch(int nk, const double* d_ks, const double* d_P0, int nl, const double* d_ThA, const double* d_ThB,
               const double* d_cprime, const double* d_invden, double* d_zbuf, double* d_Cl, cudaStream_t st);
 
+int kinterp_spline_launch(int nc, int ntau, int ns, int nf, const int* d_src, const double* d_Sc, const double* d_y,
+                          const double* d_yf, const int* d_iv, const double* d_cprime, const double* d_invden, double* d_z,
+                          double* d_Sf, cudaStream_t st);
+int kinterp_bary_launch(int nc, int ntau, int ns, int nf, const int* d_src, const double* d_Sc, const double* d_M, double* d_Sf,
+                        cudaStream_t st);
+int theta_scale_launch(int nk, int nl, int ns, const double* d_ks, const int* d_ls, int sT, int sE, double* d_Th, cudaStream_t st);
+int cl_pairs_launch(int nk, const double* d_ks, const double* d_P0, int nl, int ns, const double* d_Th, int npair,
+                    const int* d_pa, const int* d_pb, const double* d_cprime, const double* d_invden, double* d_z, double* d_Cl,
+                    cudaStream_t st);
+
 }  // namespace sbz

@@ -441,47 +441,55 @@ def spectrum_cmb(*args, **kw):
 
 
 def _spectrum_cmb_driver(modes, prob: CosmologyProblem, jl: SphericalBesselCache, ls_out=None, *, normalization="Cl",
-                         kinterp=None, Δkτ0=np.pi, xs=None, τcut=1e-2, l_limber=10, cosmo=0, taus=None):
+                         kinterp=None, Δkτ0=np.pi, xs=None, τcut=1e-2, l_limber=10, cosmo=0, taus=None, return_status=False):
+    """Grids as in the reference driver; everything after them runs in one device pipeline
+    (sbz_spectrum_cmb): coarse solve -> k-interpolation -> line of sight -> Θ scaling -> C_l."""
     modes = [modes] if isinstance(modes, str) else list(modes)
     joined = "".join(modes)
-    iT = 1 if "T" in joined else 0
-    iE = iT + 1 if "E" in joined else 0
-    iP = max(iE, iT) + 1 if "ψ" in joined else 0
+    iT = "T" in joined
+    iP = "ψ" in joined
     if kinterp is None:
         kinterp = (ChebyshevInterpolator(1e-2, 1e4, 130, fk_tanh, fkinv_tanh) if iP else ChebyshevInterpolator(1e-2, 2e3, 60))
     bg = prob.solvebg()
+    if bg.status[cosmo] != 0:
+        raise SbzError(f"background of cosmology {cosmo} failed (status {bg.status[cosmo]})")
     ls = jl.l.astype(np.float64)
     tau0 = bg.tau0[cosmo]
-    ks_fine = lingrid(kinterp.xs[-1], kinterp.xs[0], step=Δkτ0 / tau0)
+    kmin, kmax = float(np.min(kinterp.xs)), float(np.max(kinterp.xs))
+    ks_fine = lingrid(kmin, kmax, step=Δkτ0 / tau0)
     if taus is None:  # background times >= τcut, resampled on the fractional grid xs (angular.jl:280-290)
         t = bg.t(cosmo)
         t = t[t >= τcut]
         xs = cosgrid(0.0, 1.0, length=300) if xs is None else np.asarray(xs)
         taus = t[0] + (t[-1] - t[0]) * xs
     taus = L.f64(taus)
-    S, st = source_grid(prob, taus, ks_fine, kinterp, cosmo=cosmo)
-    sel = [s for s, i in ((0, iT), (1, iE), (2, iP)) if i > 0]
-    S = np.ascontiguousarray(S[:, :, sel])
-    S[-1] = 0.0
-    Th = los_integrate(S, jl.l, taus, ks_fine, jl)
-    pos, col = {}, 0
-    for name, i in (("T", iT), ("E", iE), ("ψ", iP)):
-        if i > 0:
-            pos[name] = col
-            col += 1
-    if iT:
-        Th[:, :, pos["T"]] /= ks_fine[:, None]
-    if iE:
-        Th[:, :, pos["E"]] *= np.sqrt((ls + 2) * (ls + 1) * ls * (ls - 1))[None, :] / ks_fine[:, None] ** 2
-    if iP and l_limber <= ls[-1]:
-        Th[:, :, pos["ψ"]] = los_integrate(np.ascontiguousarray(S[:, :, pos["ψ"]]), jl.l, taus, ks_fine, jl, l_limber=l_limber)
-    P0 = spectrum_primordial(ks_fine, prob, cosmo)
-    out = np.zeros((len(ls), len(modes)))
-    for im, mode in enumerate(modes):
-        A, B = pos[mode[0]], pos[mode[-1]]
-        out[:, im] = _cl_kint(np.ascontiguousarray(Th[:, :, A]), np.ascontiguousarray(Th[:, :, B]), P0, ls, ks_fine,
-                              normalization)
+    code = {"T": 0, "E": 1, "ψ": 2}
+    pa = L.i32([code[m[0]] for m in modes])
+    pb = L.i32([code[m[-1]] for m in modes])
+    if isinstance(kinterp, ChebyshevInterpolator):
+        kind, yc, wc = L.SBZ_KINTERP_BARYCENTRIC, L.f64(kinterp.ys), L.f64(kinterp.ws)
+    else:
+        kind, yc, wc = L.SBZ_KINTERP_SPLINE, L.f64(kinterp.ys), L.f64(np.zeros(len(kinterp.xs)))
+    xs_c = L.f64(kinterp.xs)
+    yf = L.f64(kinterp.f(ks_fine))
+    nl = len(ls)
+    Cl = np.zeros((len(modes), nl))
+    st = np.zeros(len(xs_c), dtype=np.int32)
+    L.check(L.lib().sbz_spectrum_cmb(prob._h, cosmo, jl._h, len(xs_c), L.dptr(xs_c), L.dptr(yc), L.dptr(wc), kind,
+                                     len(taus), L.dptr(taus), len(ks_fine), L.dptr(L.f64(ks_fine)), L.dptr(yf), len(modes),
+                                     L.iptr(pa), L.iptr(pb), int(l_limber), L.dptr(Cl), L.iptr(st)), "spectrum_cmb")
+    out = Cl.T.copy()
+    if normalization == "Dl":
+        out *= (ls * (ls + 1) / (2 * np.pi))[:, None]
     if ls_out is not None:
         ls_out = np.asarray(ls_out, dtype=np.float64)
         out = np.stack([_natural_spline(ls, out[:, i], ls_out) for i in range(len(modes))], axis=1)
-    return out
+    return (out, st) if return_status else out
+
+
+def timings(prob: CosmologyProblem):
+    """CUDA-event phase durations (ms) of the last spectrum_cmb pipeline:
+    h2d, perturbations, kinterp, los, cl, d2h, total."""
+    t = np.zeros(8)
+    L.check(L.lib().sbz_problem_timings(prob._h, L.dptr(t)), "timings")
+    return dict(zip(("h2d", "perturbations", "kinterp", "los", "cl", "d2h", "total"), t[:7]))

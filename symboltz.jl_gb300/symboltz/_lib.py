@@ -19,8 +19,10 @@ EXPORTS = (
     "sbz_default_opts", "sbz_last_error", "sbz_momentum_quadrature", "sbz_problem_create", "sbz_problem_destroy",
     "sbz_problem_nstate", "sbz_solve_bg", "sbz_bg_knots", "sbz_bg_eval", "sbz_bg_coefficients", "sbz_solve_pt", "sbz_solve_pt_device", "sbz_pt_rhs",
     "sbz_spectrum_matter", "sbz_spectrum_primordial", "sbz_bessel_create", "sbz_bessel_destroy", "sbz_bessel_eval",
-    "sbz_los_integrate", "sbz_los_integrate_device", "sbz_cl_integrate",
+    "sbz_los_integrate", "sbz_los_integrate_device", "sbz_cl_integrate", "sbz_spectrum_cmb", "sbz_problem_set_stream",
+    "sbz_problem_timings",
 )
+SBZ_KINTERP_SPLINE, SBZ_KINTERP_BARYCENTRIC = 0, 1
 
 
 class Params(C.Structure):
@@ -78,6 +80,10 @@ def lib():
     L.sbz_los_integrate.argtypes = [vp, C.c_int, dp, C.c_int, dp, C.c_int, dp, C.c_int, dp]
     L.sbz_los_integrate_device.argtypes = [vp, C.c_int, vp, C.c_int, vp, C.c_int, vp, C.c_int, vp, vp]
     L.sbz_cl_integrate.argtypes = [C.c_int, dp, dp, C.c_int, dp, dp, dp]
+    L.sbz_spectrum_cmb.argtypes = [vp, C.c_int, vp, C.c_int, dp, dp, dp, C.c_int, C.c_int, dp, C.c_int, dp, dp, C.c_int,
+                                   ip, ip, C.c_int, dp, ip]
+    L.sbz_problem_set_stream.argtypes = [vp, vp]
+    L.sbz_problem_timings.argtypes = [vp, dp]
     _lib = L
     return L
 
