@@ -268,6 +268,16 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def profile_case(args):
+    import symboltz as S
+    M = S.ΛCDM(lmax_gamma=MODEL["lmax_gamma"], lmax_nu=MODEL["lmax_nu"], lmax_h=MODEL["lmax_h"], nx=MODEL["nx"])
+    prob = S.CosmologyProblem(M, PARAMS, precision=args.precision)
+    ks, taus, ls = workload_grids(S, prob)
+    sel = ks[np.linspace(0, len(ks) - 1, 64).round().astype(int)]
+    out, st, stp = S.solvept(prob, sel, prob.opts.tau_ini, saveat=taus[::10], output="sources")
+    print(json.dumps({"profile_case": "64 modes, 200 saved times", "failed": int(np.count_nonzero(st)), "steps": int(stp.sum())}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -277,8 +287,12 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="small case for ncu section captures: 64 of the 1000 modes, 200 saved times")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile_case:
+        profile_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
