@@ -158,6 +158,20 @@ int sbz_problem_timings(const sbz_problem* pb, double* ms8);
 int sbz_cl_integrate(int nk, const double* ks, const double* P0, int nl, const double* ThA,
                      const double* ThB, double* Cl);
 
+/* No counterpart in the reference.  sbz_cl_integrate on device buffers that allocates no device
+ * memory, for callers whose memory belongs to their own pool (CUDA.jl, PyTorch's caching
+ * allocator, a fixed serving budget) and who must not see cudaMalloc/cudaFree, which sit outside
+ * that pool and synchronise the device.  d_ks, d_P0, d_ThA, d_ThB (Th[ik*nl + il]) and d_Cl[nl]
+ * are device pointers; the work is queued on `stream` (NULL: the default stream) and the call
+ * returns without waiting.  Scratch is a fixed SBZ_NOALLOC_SCRATCH_DOUBLES-double device array:
+ * sizes with 2*ceil32(nk+1) + (nk+1)*nl above it return SBZ_ERR_ARG.  All calls share that array
+ * (it keeps the last call's contents), so calls that overlap on the GPU race.  The first call on
+ * each device looks up the array's address; make it before any stream capture.  Knots that are not
+ * positive and increasing give NaN C_l (the host does not read device inputs). */
+#define SBZ_NOALLOC_SCRATCH_DOUBLES 2097152
+int sbz_cl_integrate_noalloc(int nk, const double* d_ks, const double* d_P0, int nl, const double* d_ThA,
+                             const double* d_ThB, double* d_Cl, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -743,3 +743,8 @@ int sbz_cl_integrate(int nk, const double* ks, const double* P0, int nl, const d
 }
 
 }  // extern "C"
+
+namespace sbz {
+// error reporting for entry points defined in other translation units
+int capi_fail(int code, const char* msg) { return fail(code, msg); }
+}  // namespace sbz

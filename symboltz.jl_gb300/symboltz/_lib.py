@@ -12,6 +12,7 @@ PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG, "lib", "libsymboltz_gb300.so")
 
 SBZ_OK, SBZ_MAXITERS, SBZ_DTMIN, SBZ_NONFINITE = 0, 1, 2, 3
+SBZ_ERR_ARG, SBZ_ERR_CUDA, SBZ_ERR_NOMEM, SBZ_ERR_STATE = -1, -2, -3, -4
 SBZ_FP64, SBZ_MIXED = 0, 1
 SBZ_OUT_SOURCES, SBZ_OUT_DELTA_M, SBZ_OUT_STATE = 0, 1, 2
 
@@ -19,7 +20,7 @@ EXPORTS = (
     "sbz_default_opts", "sbz_last_error", "sbz_momentum_quadrature", "sbz_problem_create", "sbz_problem_destroy",
     "sbz_problem_nstate", "sbz_solve_bg", "sbz_bg_knots", "sbz_bg_eval", "sbz_bg_coefficients", "sbz_solve_pt", "sbz_solve_pt_device", "sbz_pt_rhs",
     "sbz_spectrum_matter", "sbz_spectrum_primordial", "sbz_bessel_create", "sbz_bessel_destroy", "sbz_bessel_eval",
-    "sbz_los_integrate", "sbz_los_integrate_device", "sbz_cl_integrate", "sbz_spectrum_cmb", "sbz_problem_set_stream",
+    "sbz_los_integrate", "sbz_los_integrate_device", "sbz_cl_integrate", "sbz_cl_integrate_noalloc", "sbz_spectrum_cmb", "sbz_problem_set_stream",
     "sbz_problem_timings",
 )
 SBZ_KINTERP_SPLINE, SBZ_KINTERP_BARYCENTRIC = 0, 1
@@ -80,6 +81,8 @@ def lib():
     L.sbz_los_integrate.argtypes = [vp, C.c_int, dp, C.c_int, dp, C.c_int, dp, C.c_int, dp]
     L.sbz_los_integrate_device.argtypes = [vp, C.c_int, vp, C.c_int, vp, C.c_int, vp, C.c_int, vp, vp]
     L.sbz_cl_integrate.argtypes = [C.c_int, dp, dp, C.c_int, dp, dp, dp]
+    L.sbz_cl_integrate_noalloc.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_void_p]
     L.sbz_spectrum_cmb.argtypes = [vp, C.c_int, vp, C.c_int, dp, dp, dp, C.c_int, C.c_int, dp, C.c_int, dp, dp, C.c_int,
                                    ip, ip, C.c_int, dp, ip]
     L.sbz_problem_set_stream.argtypes = [vp, vp]
