@@ -62,7 +62,8 @@ typedef struct sbz_opts {
   int precision;            /* SBZ_FP64 or SBZ_MIXED */
   int refine_iters;         /* FP64 refinement sweeps per stage solve (SBZ_MIXED), default 1 */
   int table_points;         /* background coefficient table nodes, default 8192 */
-  int warps_per_block;      /* 0 = autotuned */
+  int warps_per_block;      /* warps per thread block (≤ 4); 0 = 4 */
+  int warps_per_mode;       /* warps integrating one mode: 1, 2 or 4; 0 = chosen from the number of modes */
 } sbz_opts;
 
 typedef struct sbz_problem sbz_problem;

@@ -118,7 +118,7 @@ extern "C" {
 void sbz_default_opts(sbz_opts* o) {
   o->bg_rtol = 1e-7; o->bg_atol = 1e-7; o->pt_rtol = 1e-5; o->pt_atol = 1e-5;
   o->tau_ini = 1e-6; o->tau_max = 100.0; o->maxiters = 100000;
-  o->precision = SBZ_MIXED; o->refine_iters = 1; o->table_points = 8192; o->warps_per_block = 0;
+  o->precision = SBZ_MIXED; o->refine_iters = 1; o->table_points = 8192; o->warps_per_block = 0; o->warps_per_mode = 0;
 }
 
 const char* sbz_last_error(void) { return g_err.c_str(); }
@@ -310,7 +310,7 @@ static int pt_run(sbz_problem* pb, int nk, const int* d_cosmo, const double* d_k
   A.refine = pb->opts.precision == SBZ_MIXED ? std::max(0, pb->opts.refine_iters) : 0;
   A.counter = pb->d_counter.as<unsigned>();
   SBZ_CUDA(cudaMemsetAsync(A.counter, 0, sizeof(unsigned), pb->stream));
-  const int r = sbz::pt_launch(A, pb->opts.precision, pb->opts.warps_per_block, pb->num_sms, pb->stream);
+  const int r = sbz::pt_launch(A, pb->opts.precision, pb->opts.warps_per_block, pb->opts.warps_per_mode, pb->num_sms, pb->stream);
   if (r != SBZ_OK) return fail(r, std::string("perturbation kernel launch: ") + cudaGetErrorString(cudaGetLastError()));
   return SBZ_OK;
 }
@@ -533,7 +533,7 @@ int sbz_spectrum_cmb(sbz_problem* pb, int cosmo, const sbz_bessel* jl, int nc, c
     A.refine = pb->opts.precision == SBZ_MIXED ? std::max(0, pb->opts.refine_iters) : 0;
     A.counter = pb->d_counter.as<unsigned>();
     SBZ_CUDA(cudaMemsetAsync(A.counter, 0, sizeof(unsigned), st));
-    r = sbz::pt_launch(A, pb->opts.precision, pb->opts.warps_per_block, pb->num_sms, st);
+    r = sbz::pt_launch(A, pb->opts.precision, pb->opts.warps_per_block, pb->opts.warps_per_mode, pb->num_sms, st);
     if (r != SBZ_OK) return fail(r, "perturbation kernel");
     // the perturbation kernel saves the sources at taus of *this* cosmology: A.taus + cosmo*ntau
   }

@@ -39,7 +39,8 @@ class Model(C.Structure):
 class Opts(C.Structure):
     _fields_ = [("bg_rtol", C.c_double), ("bg_atol", C.c_double), ("pt_rtol", C.c_double), ("pt_atol", C.c_double),
                 ("tau_ini", C.c_double), ("tau_max", C.c_double), ("maxiters", C.c_int64), ("precision", C.c_int),
-                ("refine_iters", C.c_int), ("table_points", C.c_int), ("warps_per_block", C.c_int)]
+                ("refine_iters", C.c_int), ("table_points", C.c_int), ("warps_per_block", C.c_int),
+                ("warps_per_mode", C.c_int)]
 
 
 class SbzError(RuntimeError):
