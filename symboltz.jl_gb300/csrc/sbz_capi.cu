@@ -65,6 +65,33 @@ cudaError_t up(DevBuf& b, const T* h, size_t n, cudaStream_t st) {
   return cudaMemcpyAsync(b.p, h, sizeof(T) * n, cudaMemcpyHostToDevice, st);
 }
 
+// Weights w with ∫ S = Σ_i w_i y_i for the natural cubic spline S through (X_i, y_i): the integral
+// aᵀy - cᵀz of the spline (z = second derivatives, T z = R y) is (a - Rᵀ T⁻¹ c)ᵀ y, so one
+// tridiagonal solve with the symmetric T gives the weights for every integrand on this grid.
+void spline_integral_weights(const std::vector<double>& X, std::vector<double>& w) {
+  const int n = (int)X.size();
+  w.assign(n, 0.0);
+  std::vector<double> h(n - 1);
+  for (int i = 0; i + 1 < n; ++i) { h[i] = X[i + 1] - X[i]; w[i] += 0.5 * h[i]; w[i + 1] += 0.5 * h[i]; }
+  const int m = n - 2;  // interior second derivatives z_1..z_{n-2}
+  if (m < 1) return;
+  std::vector<double> cp(m), v(m);
+  for (int j = 0; j < m; ++j) {  // Thomas on T v = c, T_jj = 2(h_{i-1}+h_i), T_j,j+1 = h_i (i = j+1)
+    const int i = j + 1;
+    const double c = (h[i - 1] * h[i - 1] * h[i - 1] + h[i] * h[i] * h[i]) / 24.0;
+    const double den = 2.0 * (h[i - 1] + h[i]) - (j > 0 ? h[i - 1] * cp[j - 1] : 0.0);
+    cp[j] = h[i] / den;
+    v[j] = (c - (j > 0 ? h[i - 1] * v[j - 1] : 0.0)) / den;
+  }
+  for (int j = m - 2; j >= 0; --j) v[j] -= cp[j] * v[j + 1];
+  for (int j = 0; j < m; ++j) {  // w -= Rᵀ v,  R y = 6 ((y_{i+1}-y_i)/h_i - (y_i-y_{i-1})/h_{i-1})
+    const int i = j + 1;
+    w[i - 1] -= 6.0 / h[i - 1] * v[j];
+    w[i] += 6.0 * (1.0 / h[i - 1] + 1.0 / h[i]) * v[j];
+    w[i + 1] -= 6.0 / h[i] * v[j];
+  }
+}
+
 int los_weights(const double* taus, int ntau, std::vector<double>& chi, std::vector<double>& w) {
   chi.resize(ntau); w.resize(ntau);
   const double t0 = taus[ntau - 1];
@@ -108,7 +135,7 @@ enum { T_H2D = 0, T_PT, T_KINTERP, T_LOS, T_CL, T_D2H, T_TOTAL };
 struct sbz_bessel {
   sbz::BesselDev J{};
   std::vector<int> ls;
-  DevBuf d_y, d_dy, d_ls;
+  DevBuf d_y, d_dy, d_yf2, d_ls;
   DevBuf d_S, d_taus, d_chi, d_w, d_ks, d_out;
   cudaStream_t stream = nullptr;
 };
@@ -480,10 +507,11 @@ int sbz_spectrum_cmb(sbz_problem* pb, int cosmo, const sbz_bessel* jl, int nc, c
   los_weights(taus, ntau, chi, w);
   std::vector<double> P0(nf);
   sbz_spectrum_primordial(pb, cosmo, nf, ks_fine, P0.data());
-  std::vector<double> Xk(nf + 1);
+  std::vector<double> Xk(nf + 1), wk;
   Xk[0] = 0; for (int i = 0; i < nf; ++i) Xk[i + 1] = ks_fine[i];
-  std::vector<double> kcp, kid;
-  spline_factors(Xk, kcp, kid);
+  spline_integral_weights(Xk, wk);
+  std::vector<double> gk(nf);  // C_l = Σ_k gk Θ_a Θ_b  (spline integral of 2/π k² P0 Θ_a Θ_b)
+  for (int i = 0; i < nf; ++i) gk[i] = wk[i + 1] * (2.0 / M_PI) * ks_fine[i] * ks_fine[i] * P0[i];
   std::vector<int> cos(nc, cosmo), ord(nc);
   std::vector<double> ti(nc, pb->bgs[cosmo].tau_start);
   std::iota(ord.begin(), ord.end(), 0);
@@ -556,11 +584,13 @@ int sbz_spectrum_cmb(sbz_problem* pb, int cosmo, const sbz_bessel* jl, int nc, c
   // 3. line-of-sight integrals and Θ scaling; gather T/E/ψ into one interleaved Θ array
   SBZ_CUDA(pb->c_Th.ensure(sizeof(double) * (size_t)nf * nl * std::max(1, nTE)));
   SBZ_CUDA(pb->c_Thp.ensure(sizeof(double) * (size_t)nf * nl));
-  if (nTE > 0 && sbz::los_launch(jl->J, const_cast<sbz_bessel*>(jl)->d_ls.as<int>(), nTE, pb->c_Sf.as<double>(), pb->c_taus.as<double>(),
-                                 pb->c_chi.as<double>(), pb->c_w.as<double>(), ntau, nf, pb->c_ks.as<double>(), nl, pb->c_Th.as<double>(), st) != 0)
+  // mixed precision: FP32 interpolation and chunk sums (the C_l target is ~1e-4); FP64 otherwise
+  auto los = pb->opts.precision == SBZ_MIXED && nl <= 1024 ? sbz::los_f32_launch : sbz::los_launch;
+  if (nTE > 0 && los(jl->J, const_cast<sbz_bessel*>(jl)->d_ls.as<int>(), nTE, pb->c_Sf.as<double>(), pb->c_taus.as<double>(),
+                     pb->c_chi.as<double>(), pb->c_w.as<double>(), ntau, nf, pb->c_ks.as<double>(), nl, pb->c_Th.as<double>(), st) != 0)
     return fail(SBZ_ERR_CUDA, "LOS kernel");
-  if (use[2] && sbz::los_launch(jl->J, const_cast<sbz_bessel*>(jl)->d_ls.as<int>(), 1, pb->c_Sp.as<double>(), pb->c_taus.as<double>(),
-                                pb->c_chi.as<double>(), pb->c_w.as<double>(), ntau, nf, pb->c_ks.as<double>(), ilim, pb->c_Thp.as<double>(), st) != 0)
+  if (use[2] && los(jl->J, const_cast<sbz_bessel*>(jl)->d_ls.as<int>(), 1, pb->c_Sp.as<double>(), pb->c_taus.as<double>(),
+                    pb->c_chi.as<double>(), pb->c_w.as<double>(), ntau, nf, pb->c_ks.as<double>(), ilim, pb->c_Thp.as<double>(), st) != 0)
     return fail(SBZ_ERR_CUDA, "LOS kernel");
   if (nTE > 0 && sbz::theta_scale_launch(nf, nl, nTE, pb->c_ks.as<double>(), const_cast<sbz_bessel*>(jl)->d_ls.as<int>(),
                                          colof[0], colof[1], pb->c_Th.as<double>(), st) != 0)
@@ -578,14 +608,10 @@ int sbz_spectrum_cmb(sbz_problem* pb, int cosmo, const sbz_bessel* jl, int nc, c
     dTh = pb->c_cl.as<double>();
     nsTh = ns_all;
   }
-  DevBuf& kfac = pb->c_kf;  // C_l spline factors
-  SBZ_CUDA(kfac.ensure(sizeof(double) * 2 * (nf + 1)));
-  SBZ_CUDA(cudaMemcpyAsync(kfac.as<double>(), kcp.data(), sizeof(double) * (nf + 1), cudaMemcpyHostToDevice, st));
-  SBZ_CUDA(cudaMemcpyAsync(kfac.as<double>() + (nf + 1), kid.data(), sizeof(double) * (nf + 1), cudaMemcpyHostToDevice, st));
-  SBZ_CUDA(pb->c_cz.ensure(sizeof(double) * (size_t)(nf + 1) * nl * npair + sizeof(double) * (size_t)nl * npair));
-  double* dCl = pb->c_cz.as<double>() + (size_t)(nf + 1) * nl * npair;
-  if (sbz::cl_pairs_launch(nf, pb->c_ks.as<double>(), pb->c_P0.as<double>(), nl, nsTh, dTh, npair, pb->c_pa.as<int>(), pb->c_pb.as<int>(),
-                           kfac.as<double>(), kfac.as<double>() + (nf + 1), pb->c_cz.as<double>(), dCl, st) != 0)
+  SBZ_CUDA(up(pb->c_kf, gk.data(), nf, st));
+  SBZ_CUDA(pb->c_cz.ensure(sizeof(double) * (size_t)nl * npair));
+  double* dCl = pb->c_cz.as<double>();
+  if (sbz::cl_dot_launch(nf, pb->c_kf.as<double>(), nl, nsTh, dTh, npair, pb->c_pa.as<int>(), pb->c_pb.as<int>(), dCl, st) != 0)
     return fail(SBZ_ERR_CUDA, "C_l kernel");
   SBZ_CUDA(cudaEventRecord(pb->ev[5], st));
   SBZ_CUDA(cudaMemcpyAsync(out_cl, dCl, sizeof(double) * nl * npair, cudaMemcpyDeviceToHost, st));
@@ -614,10 +640,12 @@ int sbz_bessel_create(int nl, const int* ls, double xmax, double dx, int hermite
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return bail("stream");
   if (c->d_y.ensure(sizeof(double) * (size_t)c->J.nx * nl) != cudaSuccess) return bail("bessel table allocation");
   if (hermite && c->d_dy.ensure(sizeof(double) * (size_t)c->J.nx * nl) != cudaSuccess) return bail("bessel table allocation");
+  if (c->d_yf2.ensure(sizeof(float2) * (size_t)c->J.nx * nl) != cudaSuccess) return bail("bessel table allocation");
   if (c->d_ls.ensure(sizeof(int) * nl) != cudaSuccess) return bail("allocation");
-  c->J.y = c->d_y.as<double>(); c->J.dy = hermite ? c->d_dy.as<double>() : nullptr;
+  c->J.y = c->d_y.as<double>(); c->J.dy = hermite ? c->d_dy.as<double>() : nullptr; c->J.yf2 = c->d_yf2.as<float2>();
   cudaMemcpyAsync(c->d_ls.p, ls, sizeof(int) * nl, cudaMemcpyHostToDevice, c->stream);
   if (sbz::bessel_build(c->J, c->d_ls.as<int>(), ls[nl - 1], c->stream) != 0) return bail("bessel kernel");
+  if (sbz::bessel_f32_build(c->J, c->stream) != 0) return bail("bessel kernel");
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return bail("bessel kernel");
   *out = c;
   return SBZ_OK;
@@ -626,7 +654,7 @@ int sbz_bessel_create(int nl, const int* ls, double xmax, double dx, int hermite
 void sbz_bessel_destroy(sbz_bessel* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
-  for (DevBuf* b : {&c->d_y, &c->d_dy, &c->d_ls, &c->d_S, &c->d_taus, &c->d_chi, &c->d_w, &c->d_ks, &c->d_out}) b->release();
+  for (DevBuf* b : {&c->d_y, &c->d_dy, &c->d_yf2, &c->d_ls, &c->d_S, &c->d_taus, &c->d_chi, &c->d_w, &c->d_ks, &c->d_out}) b->release();
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

@@ -78,7 +78,7 @@ struct CosmoDesc {
   double lnt0, idlnt;
   int ntab, pad;
   double Oc0, Ob0, Og0, On0, wh, y0, R0, As, ns, kpivot;
-  double xq[kMaxNx], Wq[kMaxNx], dlnf[kMaxNx];
+  double xq[kMaxNx], Wq[kMaxNx], dlnf[kMaxNx], ixq[kMaxNx];
   CoefExpr expr[kMaxExpr];
 };
 

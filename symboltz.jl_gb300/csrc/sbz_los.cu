@@ -125,6 +125,109 @@ __global__ void los_kernel(BesselDev J, const double* __restrict__ S, const doub
     for (int s = 0; s < NSRC; ++s) out[((size_t)ik * nl + il) * NSRC + s] = 0;
 }
 
+// Mixed-precision line of sight: one block per k, 256 threads over l (up to 4 l per thread).
+// Per chunk of 256 times the block tabulates, in FP64, what depends on (k, τ) only: the table row
+// of x = k χ, the interpolation weights and w_τ S(τ, k); the l-threads then interpolate the FP32
+// table and accumulate in FP32 over the chunk, adding chunk totals in FP64.
+constexpr int kLosChunk = 256, kLosMaxL = 4;
+template <int NSRC>
+__global__ void __launch_bounds__(256) los_f32_kernel(const float2* __restrict__ tab, int nl, double invdx, double dx, int hermite,
+                                                      const double* __restrict__ S, const double* __restrict__ chi,
+                                                      const double* __restrict__ wts, int ntau, int nk, const double* __restrict__ ks,
+                                                      int il_limber, double* __restrict__ out) {
+  __shared__ int s_i[kLosChunk];
+  __shared__ float4 s_w[kLosChunk];
+  __shared__ float s_S[kLosChunk][NSRC];
+  const int ik = blockIdx.x;
+  const double k = ks[ik];
+  double acc[kLosMaxL][NSRC];
+#pragma unroll
+  for (int m = 0; m < kLosMaxL; ++m)
+#pragma unroll
+    for (int s = 0; s < NSRC; ++s) acc[m][s] = 0;
+  for (int t0 = 0; t0 < ntau; t0 += kLosChunk) {
+    const int nt = min(kLosChunk, ntau - t0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+      const int it = t0 + t;
+      const double wpos = k * chi[it] * invdx;
+      const int i = (int)wpos;
+      const float w = (float)(wpos - i), wm1 = w - 1.0f;
+      float4 ww;
+      if (hermite) {
+        ww.x = (1.0f + 2.0f * w) * wm1 * wm1; ww.y = w * w * (3.0f - 2.0f * w);
+        ww.z = (float)(w * wm1 * wm1 * dx); ww.w = (float)(w * w * wm1 * dx);
+      } else {
+        ww.x = 1.0f - w; ww.y = w; ww.z = 0.0f; ww.w = 0.0f;
+      }
+      s_i[t] = i; s_w[t] = ww;
+      const double wt = wts[it];
+#pragma unroll
+      for (int s = 0; s < NSRC; ++s) s_S[t][s] = (float)(wt * S[((size_t)it * nk + ik) * NSRC + s]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < kLosMaxL; ++m) {
+      const int il = threadIdx.x + blockDim.x * m;
+      if (il < il_limber) {
+        float p[NSRC];
+#pragma unroll
+        for (int s = 0; s < NSRC; ++s) p[s] = 0.0f;
+#pragma unroll 4
+        for (int t = 0; t < nt; ++t) {
+          const int i = s_i[t];
+          const float4 ww = s_w[t];
+          const float2 a = __ldg(tab + (size_t)i * nl + il), b = __ldg(tab + (size_t)(i + 1) * nl + il);
+          const float j = fmaf(ww.x, a.x, fmaf(ww.y, b.x, fmaf(ww.z, a.y, ww.w * b.y)));
+#pragma unroll
+          for (int s = 0; s < NSRC; ++s) p[s] = fmaf(s_S[t][s], j, p[s]);
+        }
+#pragma unroll
+        for (int s = 0; s < NSRC; ++s) acc[m][s] += (double)p[s];
+      }
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < kLosMaxL; ++m) {
+    const int il = threadIdx.x + blockDim.x * m;
+    if (il < il_limber)
+#pragma unroll
+      for (int s = 0; s < NSRC; ++s) out[((size_t)ik * nl + il) * NSRC + s] = acc[m][s];
+  }
+  for (int il = il_limber + threadIdx.x; il < nl; il += blockDim.x)
+#pragma unroll
+    for (int s = 0; s < NSRC; ++s) out[((size_t)ik * nl + il) * NSRC + s] = 0;
+}
+
+__global__ void bessel_f32_kernel(BesselDev J) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)J.nx * J.nl) return;
+  J.yf2[t] = make_float2((float)J.y[t], J.dy ? (float)J.dy[t] : 0.0f);
+}
+
+// C_l as a weighted sum over k: one block per (pair, l), FP64 throughout.
+__global__ void __launch_bounds__(256) cl_dot_kernel(int nk, const double* __restrict__ g, int nl, int ns,
+                                                     const double* __restrict__ Th, const int* __restrict__ pa,
+                                                     const int* __restrict__ pb, double* __restrict__ Cl) {
+  const int il = blockIdx.x % nl, q = blockIdx.x / nl;
+  const int A = pa[q], B = pb[q];
+  double sum = 0;
+  for (int i = threadIdx.x; i < nk; i += blockDim.x) {
+    const size_t o = ((size_t)i * nl + il) * ns;
+    sum = fma(g[i] * Th[o + A], Th[o + B], sum);
+  }
+  __shared__ double red[8];
+#pragma unroll
+  for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+    Cl[blockIdx.x] = tot;
+  }
+}
+
 // Limber approximation (src/observables/angular.jl:154-178); one thread per (k, l >= l_limber).
 __global__ void limber_kernel(const int* __restrict__ ls, int nl, int il_limber, int nsrc, const double* __restrict__ S,
                               const double* __restrict__ taus, const double* __restrict__ chi, int ntau, int nk,
@@ -263,43 +366,6 @@ __global__ void theta_scale(int nk, int nl, int ns, const double* __restrict__ k
   if (sE >= 0) Th[t * ns + sE] *= sqrt((l + 2) * (l + 1) * l * (l - 1)) / (k * k);
 }
 
-// C_l from interleaved Θ [(ik*nl + il)*ns + s] for pairs (a, b): same spline integral as cl_kernel.
-__global__ void cl_pairs_kernel(int nk, const double* __restrict__ ks, const double* __restrict__ P0, int nl, int ns,
-                                const double* __restrict__ Th, int npair, const int* __restrict__ pa, const int* __restrict__ pb,
-                                const double* __restrict__ cprime, const double* __restrict__ invden,
-                                double* __restrict__ zbuf, double* __restrict__ Cl) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nl * npair) return;
-  const int il = t % nl, q = t / nl;
-  const int A = pa[q], Bq = pb[q];
-  const int np = nk + 1;
-  const int stride = nl * npair;
-  auto X = [&](int i) { return i == 0 ? 0.0 : ks[i - 1]; };
-  auto Y = [&](int i) {
-    if (i == 0) return 0.0;
-    const size_t o = ((size_t)(i - 1) * nl + il) * ns;
-    return (2.0 / M_PI) * ks[i - 1] * ks[i - 1] * P0[i - 1] * Th[o + A] * Th[o + Bq];
-  };
-  double* z = zbuf + t;
-  double yprev = Y(0), ycur = Y(1), dprev = 0;
-  for (int i = 1; i <= np - 2; ++i) {
-    const double ynext = Y(i + 1);
-    const double h0 = X(i) - X(i - 1), h1 = X(i + 1) - X(i);
-    const double d = (6 * ((ynext - ycur) / h1 - (ycur - yprev) / h0) - h0 * dprev) * invden[i];
-    z[(size_t)i * stride] = d;
-    dprev = d; yprev = ycur; ycur = ynext;
-  }
-  double znext = 0, sum = 0, ynext = Y(np - 1);
-  for (int i = np - 2; i >= 0; --i) {
-    const double zi = (i >= 1) ? z[(size_t)i * stride] - cprime[i] * znext : 0.0;
-    const double yi = Y(i);
-    const double h = X(i + 1) - X(i);
-    sum += h * (yi + ynext) * 0.5 - h * h * h * (zi + znext) / 24.0;
-    znext = zi; ynext = yi;
-  }
-  Cl[t] = sum;
-}
-
 }  // namespace
 
 int kinterp_spline_launch(int nc, int ntau, int ns, int nf, const int* d_src, const double* d_Sc, const double* d_y,
@@ -325,17 +391,38 @@ int theta_scale_launch(int nk, int nl, int ns, const double* d_ks, const int* d_
   return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }
 
-int cl_pairs_launch(int nk, const double* d_ks, const double* d_P0, int nl, int ns, const double* d_Th, int npair,
-                    const int* d_pa, const int* d_pb, const double* d_cprime, const double* d_invden, double* d_z, double* d_Cl,
-                    cudaStream_t st) {
-  const int total = nl * npair;
-  cl_pairs_kernel<<<(total + 127) / 128, 128, 0, st>>>(nk, d_ks, d_P0, nl, ns, d_Th, npair, d_pa, d_pb, d_cprime, d_invden, d_z, d_Cl);
-  return cudaGetLastError() == cudaSuccess ? 0 : -2;
-}
-
 int bessel_build(BesselDev& J, const int* d_ls, int Lmax, cudaStream_t st) {
   const int N = J.nx - 1;
   bessel_table_kernel<<<(N + 127) / 128, 128, 0, st>>>(J, d_ls, Lmax);
+  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+int bessel_f32_build(const BesselDev& J, cudaStream_t st) {
+  const size_t total = (size_t)J.nx * J.nl;
+  bessel_f32_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(J);
+  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+int los_f32_launch(const BesselDev& J, const int* d_ls, int nsrc, const double* d_S, const double* d_taus, const double* d_chi,
+                   const double* d_w, int ntau, int nk, const double* d_ks, int il_limber, double* d_out, cudaStream_t st) {
+  if (!J.yf2 || il_limber > 256 * kLosMaxL || nk <= 0) return -1;
+  switch (nsrc) {
+    case 1: los_f32_kernel<1><<<nk, 256, 0, st>>>(J.yf2, J.nl, J.invdx, J.dx, J.hermite, d_S, d_chi, d_w, ntau, nk, d_ks, il_limber, d_out); break;
+    case 2: los_f32_kernel<2><<<nk, 256, 0, st>>>(J.yf2, J.nl, J.invdx, J.dx, J.hermite, d_S, d_chi, d_w, ntau, nk, d_ks, il_limber, d_out); break;
+    case 3: los_f32_kernel<3><<<nk, 256, 0, st>>>(J.yf2, J.nl, J.invdx, J.dx, J.hermite, d_S, d_chi, d_w, ntau, nk, d_ks, il_limber, d_out); break;
+    default: return -1;
+  }
+  const int nlim = J.nl - il_limber;
+  if (nlim > 0) {
+    const int tot = nk * nlim;
+    limber_kernel<<<(tot + 127) / 128, 128, 0, st>>>(d_ls, J.nl, il_limber, nsrc, d_S, d_taus, d_chi, ntau, nk, d_ks, d_out);
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+int cl_dot_launch(int nk, const double* d_g, int nl, int ns, const double* d_Th, int npair, const int* d_pa, const int* d_pb,
+                  double* d_Cl, cudaStream_t st) {
+  cl_dot_kernel<<<nl * npair, 256, 0, st>>>(nk, d_g, nl, ns, d_Th, d_pa, d_pb, d_Cl);
   return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }
 

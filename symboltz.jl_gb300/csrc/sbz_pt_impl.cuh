@@ -55,7 +55,7 @@ constexpr int kWF = 2 * kMaxFun;  // functional weights per set: Œ® terms then Œ
 constexpr int kMaxT = 4;          // coefficient sets evaluated in one pass (the four stage times)
 constexpr int kNSets = 6;         // J (step start), three stage times, step end, output time
 
-static_assert(sizeof(ModelDesc) % 4 == 0 && sizeof(CompDesc) % 4 == 0, "word copies");
+static_assert(sizeof(ModelDesc) % 4 == 0 && sizeof(CompDesc) % 4 == 0 && sizeof(CosmoDesc) % 4 == 0, "word copies");
 
 // one coefficient set: operator coefficients, their œÑ-derivatives, functional weights
 struct CSet {
@@ -70,15 +70,20 @@ struct ModeMem {
   ST r[NM + 1];       // structured-solve right-hand side / work vector
   ST u[NM];           // W‚Åª¬π r result
   ST dinv[NM], sub[NM], sup[NM], mfw[NM], dd[NM];
+  ST fA[5][NM], bA[5][NM], bP[NM];   // warp-scan multipliers of the chain eliminations, per row
+  ST cf[2][kMaxChains];              // forward-eliminated first row of each chain, per vector
+  int16_t att[NM];                   // head row a chain row's back substitution depends on, or -1
+  int hatt[8];                       // chain attached to head row 3 + q, or -1
   ST Z1[NM + 1], Z2[NM + 1];
-  ST H[64];
+  ST H[64], Hinv[64];
   ST hmul[kMaxChains], hcorr[kMaxChains];
-  int piv[8];
+  ST wS[kWF], fS[4];  // Jacobian-set functional weights and Œ¶Ãá coefficients in solve precision
   CSet cs[kNSets];
   double hv[kMaxT][8], hd[kMaxT][8];     // table interpolants per time: a, ‚Ñã, Œ∫Ãá, c_s¬≤, e^{-Œ∫}, Œ∫Ãà, Œ∫‚Éõ
   double B[kMaxT][B_COUNT], dB[kMaxT][B_COUNT];
   double src[4];      // e^{-Œ∫}, Œ∫Ãà, Œ∫‚Éõ at an output time
   double red[2][NW];  // ping-pong group reductions
+  CosmoDesc cdesc;    // the current mode's cosmology (coefficient expressions, bin momenta)
   int item;
 };
 
@@ -93,9 +98,11 @@ struct Grp {
   }
 };
 
-// thread of the group that runs serial task j (chains, head blocks): spread over the warps
+// Component held by thread gt in slot s.  Slot 0 is the identity (the head rows with their extra
+// couplings sit in warp 0); later slots start at the last warp, so the partial last slot does not
+// land on warp 0 as well.
 template <int NW>
-__device__ __forceinline__ int task_thread(int j) { return (j % NW) * 32 + j / NW; }
+__device__ __forceinline__ int comp_of(int gt, int s) { return s * 32 * NW + ((gt + 32 * s) & (32 * NW - 1)); }
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -103,8 +110,14 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-template <int NW, int NSL, typename ST>
-__device__ __forceinline__ double group_sum(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, double v) {
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  return v;
+}
+
+template <int NW, int NSL, typename ST, typename T>
+__device__ __forceinline__ T group_sum(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, T v) {
   v = warp_sum(v);
   if constexpr (NW == 1) {
     __syncwarp();
@@ -112,9 +125,9 @@ __device__ __forceinline__ double group_sum(const Grp<NW>& g, ModeMem<NW, NSL, S
   } else {
     if (g.lane == 0) W.red[g.rp][g.wq] = v;
     g.sync();
-    double s = 0;
+    T s = 0;
 #pragma unroll
-    for (int w = 0; w < NW; ++w) s += W.red[g.rp][w];
+    for (int w = 0; w < NW; ++w) s += (T)W.red[g.rp][w];
     g.rp ^= 1;
     return s;
   }
@@ -123,7 +136,11 @@ __device__ __forceinline__ double group_sum(const Grp<NW>& g, ModeMem<NW, NSL, S
 template <typename ST>
 __device__ __forceinline__ ST rcp(ST v);
 template <>
-__device__ __forceinline__ float rcp<float>(float v) { return __frcp_rn(v); }
+__device__ __forceinline__ float rcp<float>(float v) {  // approximate reciprocal: the FP32 solve is a preconditioner
+  float r;
+  asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(v));
+  return r;
+}
 template <>
 __device__ __forceinline__ double rcp<double>(double v) { return 1.0 / v; }
 
@@ -175,10 +192,10 @@ __device__ __forceinline__ void coef_eval(const Grp<NW>& g, ModeMem<NW, NSL, ST>
       else {
         const int b = j - 3;
         const double xj = cd->xq[b], y0a = cd->y0 * a;
-        const double E = sqrt(xj * xj + y0a * y0a);
-        const double iE = 1.0 / E;
+        const double E2 = xj * xj + y0a * y0a;
+        const double iE = rsqrt(E2), E = E2 * iE;
         const double dE = cd->y0 * y0a * da * iE;
-        const double ixj = 1.0 / xj;
+        const double ixj = cd->ixq[b];
         W.B[q][B_Q + b] = xj * iE; W.B[q][B_IQ + b] = E * ixj; W.B[q][B_E + b] = E; W.B[q][B_IE + b] = iE;
         W.dB[q][B_Q + b] = -xj * dE * iE * iE; W.dB[q][B_IQ + b] = dE * ixj; W.dB[q][B_E + b] = dE; W.dB[q][B_IE + b] = -dE * iE * iE;
         continue;
@@ -255,7 +272,7 @@ __device__ __forceinline__ void matvec(int gt, const double* x, const CSet& C, c
   const double k34 = 0.75 * k;
 #pragma unroll
   for (int s = 0; s < NSL; ++s) {
-    const int i = gt + 32 * NW * s;
+    const int i = comp_of<NW>(gt, s);
     double o = 0;
     if (i < M.n) {
       const CompDesc& D = comps[i];
@@ -280,7 +297,7 @@ __device__ __forceinline__ void matvec_dtau(int gt, const double* x, const CSet&
   const double k34 = 0.75 * k;
 #pragma unroll
   for (int s = 0; s < NSL; ++s) {
-    const int i = gt + 32 * NW * s;
+    const int i = comp_of<NW>(gt, s);
     double o = 0;
     if (i < M.n) {
       const CompDesc& D = comps[i];
@@ -294,99 +311,192 @@ __device__ __forceinline__ void matvec_dtau(int gt, const double* x, const CSet&
 
 // ------------------------------------------------------------------------------------------
 // structured factorisation of M = s I - B and its solves
+//
+// Chains of at most 32 rows are eliminated with warp scans (lane j holds row last - j): the
+// forward elimination c_i = r_i - m_i c_{i+1} runs up the lanes, the back substitution
+// z_i = d_i c_i - d_i b_i z_{i-1} down the lanes; both are affine recurrences whose Kogge-Stone
+// multipliers depend only on the factorisation and are tabulated per row (fA, bA, bP) once per
+// step.  The back substitution is run with a zero head value; the head value h enters linearly as
+// z_i += P_i h (P_i = bP[i]), which the consumers of a solution add for their own rows.  A solve is
+// then one scan phase (both directions), one head phase and two barriers.  Longer chains fall
+// back to one thread per chain with an exact back substitution.  The 8x8 head is inverted explicitly
+// (Gauss-Jordan with partial pivoting, one row per lane), so a head solve is an 8-term product.
 __device__ __forceinline__ int head_local(int i) { return (i >= 3 && i <= 10) ? i - 3 : -1; }
 
 template <typename ST>
 struct Factor {
   ST is, ihc;
-  double S00, S01, S10, S11;  // inverse of I - V·µÄ M‚Åª¬π U
+  ST S00, S01, S10, S11;  // inverse of I - V·µÄ M‚Åª¬π U
 };
+
+template <typename T>
+__device__ __forceinline__ T shfl_up_(T v, int d) { return __shfl_up_sync(FULL, v, d); }
+
+// chains (2p, 2p+1) for pass p; lane j holds row last - j (forward) or first + j (back)
+struct ChainPair {
+  int f0, l0, a0, f1, l1, a1;  // first, last, attach (a = -2: absent chain)
+};
+__device__ __forceinline__ ChainPair chain_pair(const ModelDesc& M, int p) {
+  ChainPair c;
+  const int c0 = 2 * p, c1 = 2 * p + 1;
+  c.f0 = M.chFirst[c0]; c.l0 = M.chLast[c0]; c.a0 = M.chAttach[c0];
+  if (c1 < M.nchain) { c.f1 = M.chFirst[c1]; c.l1 = M.chLast[c1]; c.a1 = M.chAttach[c1]; }
+  else { c.f1 = 0; c.l1 = -1; c.a1 = -2; }
+  return c;
+}
 
 // M‚Åª¬π applied in place to NV vectors (input complete; ends with a group barrier).
 template <int NV, int NW, int NSL, typename ST>
-__device__ __forceinline__ void solve_M(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const ModelDesc& M, const Factor<ST>& F, ST* v0, ST* v1) {
-  const int gt = g.gt;
+__device__ __forceinline__ void solve_M(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const ModelDesc& M, const Factor<ST>& F,
+                                        bool scan, ST* v0, ST* v1) {
+  const int gt = g.gt, lane = g.lane;
+  const int npair = (M.nchain + 1) >> 1;
   // forward elimination along the chains, truncation end first
-  int ch = -1;
-  for (int c = 0; c < M.nchain; ++c) if (task_thread<NW>(c) == gt) ch = c;
-  if (ch >= 0) {
-    const int first = M.chFirst[ch], last = M.chLast[ch];
-    ST c0 = v0[last], c1 = NV > 1 ? v1[last] : ST(0);
-#pragma unroll 4
-    for (int i = last - 1; i >= first; --i) {
-      const ST m = W.mfw[i];
-      c0 = v0[i] - m * c0; v0[i] = c0;
-      if (NV > 1) { c1 = v1[i] - m * c1; v1[i] = c1; }
+  if (scan) {
+    for (int p = g.wq; p < npair; p += NW) {
+      const ChainPair c = chain_pair(M, p);
+      const int i0 = c.l0 - lane, i1 = c.l1 - lane;
+      const bool on0 = i0 >= c.f0, on1 = i1 >= c.f1;
+      ST m0[5], m1[5], n0[5], n1[5];
+#pragma unroll
+      for (int q = 0; q < 5; ++q) {
+        m0[q] = on0 ? W.fA[q][i0] : ST(0); m1[q] = on1 ? W.fA[q][i1] : ST(0);
+        n0[q] = on0 ? W.bA[q][i0] : ST(0); n1[q] = on1 ? W.bA[q][i1] : ST(0);
+      }
+      const ST d0 = on0 ? W.dinv[i0] : ST(0), d1 = on1 ? W.dinv[i1] : ST(0);
+      ST x0 = on0 ? v0[i0] : ST(0), x1 = on1 ? v0[i1] : ST(0);
+      ST y0 = (NV > 1 && on0) ? v1[i0] : ST(0), y1 = (NV > 1 && on1) ? v1[i1] : ST(0);
+#pragma unroll
+      for (int q = 0; q < 5; ++q) {  // forward elimination, up the lanes
+        const int d = 1 << q;
+        const ST px0 = shfl_up_(x0, d), px1 = shfl_up_(x1, d);
+        x0 += m0[q] * px0; x1 += m1[q] * px1;
+        if (NV > 1) { const ST py0 = shfl_up_(y0, d), py1 = shfl_up_(y1, d); y0 += m0[q] * py0; y1 += m1[q] * py1; }
+      }
+      if (i0 == c.f0 && c.a0 >= 0) { W.cf[0][2 * p] = x0; if (NV > 1) W.cf[1][2 * p] = y0; }
+      if (i1 == c.f1 && c.a1 >= 0) { W.cf[0][2 * p + 1] = x1; if (NV > 1) W.cf[1][2 * p + 1] = y1; }
+      x0 *= d0; x1 *= d1;
+      if (NV > 1) { y0 *= d0; y1 *= d1; }
+#pragma unroll
+      for (int q = 0; q < 5; ++q) {  // back substitution with a zero head value, down the lanes
+        const int d = 1 << q;
+        const ST px0 = __shfl_down_sync(FULL, x0, d), px1 = __shfl_down_sync(FULL, x1, d);
+        x0 += n0[q] * px0; x1 += n1[q] * px1;
+        if (NV > 1) {
+          const ST py0 = __shfl_down_sync(FULL, y0, d), py1 = __shfl_down_sync(FULL, y1, d);
+          y0 += n0[q] * py0; y1 += n1[q] * py1;
+        }
+      }
+      if (on0) { v0[i0] = x0; if (NV > 1) v1[i0] = y0; }
+      if (on1) { v0[i1] = x1; if (NV > 1) v1[i1] = y1; }
     }
-    const int at = M.chAttach[ch];
-    if (at >= 0) {
-      const ST hm = W.hmul[ch];
-      v0[at] -= hm * c0;
-      if (NV > 1) v1[at] -= hm * c1;
+    if (g.wq == NW - 1 && (lane == 16 || lane == 17)) {  // CDM: [[s, 1], [0, s+‚Ñã]]
+      ST* v = lane == 16 ? v0 : v1;
+      if (lane == 16 || NV > 1) {
+        const ST zt = v[2] * F.ihc;
+        v[2] = zt;
+        v[1] = (v[1] - zt) * F.is;
+      }
+    } else if (g.wq == NW - 1 && lane == 18) {
+      v0[0] *= F.is;
+      if (NV > 1) v1[0] *= F.is;
+    }
+    g.sync();
+    if (g.wq == 0 && lane < 8) {  // 8x8 head with the chains' couplings: explicit inverse
+      const int ch = W.hatt[lane];
+      ST b0 = v0[3 + lane], b1 = NV > 1 ? v1[3 + lane] : ST(0);
+      if (ch >= 0) { const ST hm = W.hmul[ch]; b0 -= hm * W.cf[0][ch]; if (NV > 1) b1 -= hm * W.cf[1][ch]; }
+      ST o0 = 0, o1 = 0;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const ST hq = W.Hinv[lane * 8 + q];
+        o0 += hq * __shfl_sync(0xffu, b0, q);
+        if (NV > 1) o1 += hq * __shfl_sync(0xffu, b1, q);
+      }
+      v0[3 + lane] = o0;
+      if (NV > 1) v1[3 + lane] = o1;
+    }
+    g.sync();
+    return;
+  } else {
+    for (int ch = gt; ch < M.nchain; ch += 32 * NW) {
+      const int first = M.chFirst[ch], last = M.chLast[ch];
+      ST c0 = v0[last], c1 = NV > 1 ? v1[last] : ST(0);
+      for (int i = last - 1; i >= first; --i) {
+        const ST m = W.mfw[i];
+        c0 = v0[i] - m * c0; v0[i] = c0;
+        if (NV > 1) { c1 = v1[i] - m * c1; v1[i] = c1; }
+      }
+      const int at = M.chAttach[ch];
+      if (at >= 0) { const ST hm = W.hmul[ch]; v0[at] -= hm * c0; if (NV > 1) v1[at] -= hm * c1; }
     }
   }
   g.sync();
-  if (gt == task_thread<NW>(0)) {  // 8x8 head: LU solve
+  if (g.wq == 0) {
+    if (lane < 8) {  // 8x8 head: explicit inverse
+      ST o0 = 0, o1 = 0;
 #pragma unroll
-    for (int vv = 0; vv < NV; ++vv) {
-      ST* v = vv == 0 ? v0 : v1;
-      ST b[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) b[j] = v[3 + j];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) { const int p = W.piv[j]; if (p != j) { ST t = b[j]; b[j] = b[p]; b[p] = t; } }
-#pragma unroll
-      for (int i = 1; i < 8; ++i) {
-        ST s = b[i];
-#pragma unroll
-        for (int j = 0; j < i; ++j) s -= W.H[i * 8 + j] * b[j];
-        b[i] = s;
+      for (int q = 0; q < 8; ++q) {
+        const ST hq = W.Hinv[lane * 8 + q];
+        o0 += hq * v0[3 + q];
+        if (NV > 1) o1 += hq * v1[3 + q];
       }
-#pragma unroll
-      for (int i = 7; i >= 0; --i) {
-        ST s = b[i];
-#pragma unroll
-        for (int j = i + 1; j < 8; ++j) s -= W.H[i * 8 + j] * b[j];
-        b[i] = s * W.H[i * 8 + i];  // diagonal holds the reciprocal pivot
+      __syncwarp(0xffu);
+      v0[3 + lane] = o0;
+      if (NV > 1) v1[3 + lane] = o1;
+    } else if (lane == 8 || lane == 9) {  // CDM: [[s, 1], [0, s+‚Ñã]]
+      ST* v = lane == 8 ? v0 : v1;
+      if (lane == 8 || NV > 1) {
+        const ST zt = v[2] * F.ihc;
+        v[2] = zt;
+        v[1] = (v[1] - zt) * F.is;
       }
-#pragma unroll
-      for (int j = 0; j < 8; ++j) v[3 + j] = b[j];
+    } else if (lane == 10) {
+      v0[0] *= F.is;
+      if (NV > 1) v1[0] *= F.is;
     }
-  } else if (gt == task_thread<NW>(1)) {  // CDM: [[s, 1], [0, s+‚Ñã]]
-#pragma unroll
-    for (int vv = 0; vv < NV; ++vv) {
-      ST* v = vv == 0 ? v0 : v1;
-      const ST zt = v[2] * F.ihc;
-      v[2] = zt;
-      v[1] = (v[1] - zt) * F.is;
-    }
-  } else if (gt == task_thread<NW>(2)) {
-    v0[0] *= F.is;
-    if (NV > 1) v1[0] *= F.is;
   }
   g.sync();
-  if (ch >= 0) {  // back substitution away from the head
-    const int first = M.chFirst[ch], last = M.chLast[ch], at = M.chAttach[ch];
-    ST z0 = at >= 0 ? v0[at] : ST(0), z1 = (NV > 1 && at >= 0) ? v1[at] : ST(0);
-#pragma unroll 4
-    for (int i = first; i <= last; ++i) {
-      const ST sb = W.sub[i], di = W.dinv[i];
-      z0 = (v0[i] - sb * z0) * di; v0[i] = z0;
-      if (NV > 1) { z1 = (v1[i] - sb * z1) * di; v1[i] = z1; }
+  // back substitution away from the head (one thread per chain)
+  {
+    for (int ch = gt; ch < M.nchain; ch += 32 * NW) {
+      const int first = M.chFirst[ch], last = M.chLast[ch], at = M.chAttach[ch];
+      ST z0 = at >= 0 ? v0[at] : ST(0), z1 = (NV > 1 && at >= 0) ? v1[at] : ST(0);
+      for (int i = first; i <= last; ++i) {
+        const ST sb = W.sub[i], di = W.dinv[i];
+        z0 = (v0[i] - sb * z0) * di; v0[i] = z0;
+        if (NV > 1) { z1 = (v1[i] - sb * z1) * di; v1[i] = z1; }
+      }
     }
   }
   g.sync();
 }
 
+// Functionals in solve precision from the factorisation's weight copy: Œ®(v), Œ¥œÅ sum, Œ¶Ãá.
+template <int NW, int NSL, typename ST>
+__device__ __forceinline__ void functionals_st(const ModeMem<NW, NSL, ST>& W, const ST* v, const ModelDesc& M, ST& psi, ST& phd) {
+  const int lane = threadIdx.x & 31;
+  ST t = 0;
+  if (lane < M.npsi) t = W.wS[lane] * v[M.psiComp[lane]];
+  else if (lane >= kMaxFun && lane - kMaxFun < M.nrho) t = W.wS[lane] * v[M.rhoComp[lane - kMaxFun]];
+#pragma unroll
+  for (int o = 8; o; o >>= 1) t += __shfl_xor_sync(FULL, t, o);
+  psi = __shfl_sync(FULL, t, 0);
+  const ST rho = __shfl_sync(FULL, t, 16);
+  phd = W.fS[0] * rho + W.fS[1] * v[0] + W.fS[2] * psi;
+}
+
 template <int NW, int NSL, typename ST>
 __device__ __forceinline__ void factorize(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, Factor<ST>& F, const CSet& C,
-                          const CompDesc* __restrict__ comps, const ModelDesc& M, double k, double h, double s) {
-  const int gt = g.gt;
+                                          const CompDesc* __restrict__ comps, const ModelDesc& M, double k, double h,
+                                          double s, bool scan) {
+  const int gt = g.gt, lane = g.lane;
   const double* cv = C.cv;
-  // per-row inputs, all threads: diagonal s - (dg + tr) and the two chain couplings
+  // per-row inputs, all threads: diagonal s - (dg + tr), the two chain couplings, the rank-2
+  // columns; the functional weights in solve precision
 #pragma unroll
   for (int sl = 0; sl < NSL; ++sl) {
-    const int i = gt + 32 * NW * sl;
+    const int i = comp_of<NW>(gt, sl);
     if (i < M.n) {
       const CompDesc& D = comps[i];
       const double spv = cv[D.sp];
@@ -397,10 +507,10 @@ __device__ __forceinline__ void factorize(const Grp<NW>& g, ModeMem<NW, NSL, ST>
       W.Z2[i] = (ST)cv[D.psid];
     }
   }
+  for (int q = gt; q < kWF; q += 32 * NW) W.wS[q] = (ST)C.w[q];
+  if (gt < 3) W.fS[gt] = (ST)cv[gt == 0 ? CV_PA : gt == 1 ? CV_PB : CV_MH];
   g.sync();
-  int ch = -1;
-  for (int c = 0; c < M.nchain; ++c) if (task_thread<NW>(c) == gt) ch = c;
-  if (ch >= 0) {  // chain LU from the truncation end (precision ST)
+  for (int ch = gt; ch < M.nchain; ch += 32 * NW) {  // chain LU from the truncation end (precision ST)
     const int first = M.chFirst[ch], last = M.chLast[ch], at = M.chAttach[ch];
     ST dn = rcp<ST>(W.dd[last]);
     W.dinv[last] = dn; W.mfw[last] = 0;
@@ -418,8 +528,8 @@ __device__ __forceinline__ void factorize(const Grp<NW>& g, ModeMem<NW, NSL, ST>
       W.hcorr[ch] = hm * W.sub[first];
     }
   }
-  if (g.wq == NW - 1 && g.lane >= 16 && g.lane < 24) {  // assemble head row 3 + j
-    const int j = g.lane - 16, r = 3 + j;
+  if (g.wq == NW - 1 && lane >= 16 && lane < 24) {  // assemble head row 3 + j
+    const int j = lane - 16, r = 3 + j;
     const double k34 = 0.75 * k;
     const CompDesc& D = comps[r];
     double row[8];
@@ -439,51 +549,115 @@ __device__ __forceinline__ void factorize(const Grp<NW>& g, ModeMem<NW, NSL, ST>
     for (int q = 0; q < 8; ++q) W.H[j * 8 + q] = (ST)row[q];
   }
   g.sync();
-  if (gt == task_thread<NW>(0)) {  // LU with partial pivoting; reciprocal pivots on the diagonal
-    W.H[4 * 8 + 4] -= W.hcorr[0];  // F2 (Schur complement of the F tail)
-    W.H[7 * 8 + 7] -= W.hcorr[1];  // G2 (G tail)
-    for (int kk = 0; kk < 8; ++kk) {
-      int p = kk; ST mx = fabs(W.H[kk * 8 + kk]);
-      for (int i = kk + 1; i < 8; ++i) { const ST v = fabs(W.H[i * 8 + kk]); if (v > mx) { mx = v; p = i; } }
-      W.piv[kk] = p;
-      if (p != kk) for (int j = 0; j < 8; ++j) { const ST t = W.H[kk * 8 + j]; W.H[kk * 8 + j] = W.H[p * 8 + j]; W.H[p * 8 + j] = t; }
-      const ST ip = ST(1) / W.H[kk * 8 + kk];
-      W.H[kk * 8 + kk] = ip;
-      for (int i = kk + 1; i < 8; ++i) {
-        const ST l = W.H[i * 8 + kk] * ip;
-        W.H[i * 8 + kk] = l;
-        for (int j = kk + 1; j < 8; ++j) W.H[i * 8 + j] -= l * W.H[kk * 8 + j];
+  const int npair = (M.nchain + 1) >> 1;
+  if (scan) {
+    // Kogge-Stone multipliers of both chain recurrences, one chain row per lane
+    for (int p = g.wq; p < npair; p += NW) {
+#pragma unroll
+      for (int hc = 0; hc < 2; ++hc) {
+        const int ch = 2 * p + hc;
+        const bool live = ch < M.nchain;
+        const int first = live ? M.chFirst[ch] : 0, last = live ? M.chLast[ch] : -1;
+        {  // forward: lane j = row last - j, element (a_j = -m_j, c_j); a_0 = 0
+          const int i = last - lane;
+          const bool on = i >= first;
+          ST a = (on && lane > 0) ? -W.mfw[i] : ST(0);
+#pragma unroll
+          for (int q = 0; q < 5; ++q) {
+            const int d = 1 << q;
+            const ST ap = shfl_up_(a, d);
+            if (on) W.fA[q][i] = lane >= d ? a : ST(0);
+            if (lane >= d) a *= ap;
+          }
+        }
+        {  // back: lane j = row last - j, element (a_j = -d_j b_j, d_j c_j); the head value
+           // follows the last lane (row first), so the scan runs down the lanes
+          const int i = last - lane, L = last - first + 1;
+          const bool on = i >= first;
+          ST a = on ? -W.dinv[i] * W.sub[i] : ST(0);
+#pragma unroll
+          for (int q = 0; q < 5; ++q) {
+            const int d = 1 << q;
+            const ST ap = __shfl_down_sync(FULL, a, d);
+            const bool in = lane + d < L;
+            if (on) W.bA[q][i] = in ? a : ST(0);
+            if (in) a *= ap;
+          }
+          if (on) W.bP[i] = a;  // ‚àÇz_i/‚àÇh
+        }
       }
+    }
+  }
+  if (g.wq == 0) {  // head inverse: Gauss-Jordan with partial pivoting, lane r holds row r
+    const int r = lane;
+    ST a[8], e[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) { a[q] = r < 8 ? W.H[r * 8 + q] : ST(0); e[q] = (q == r) ? ST(1) : ST(0); }
+    if (r == 4) a[4] -= W.hcorr[0];  // F2 (Schur complement of the F tail)
+    if (r == 7) a[7] -= W.hcorr[1];  // G2 (G tail)
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) {
+      ST val = (r >= kk && r < 8) ? fabs(a[kk]) : ST(-1);
+      int idx = r;
+#pragma unroll
+      for (int o = 1; o < 8; o <<= 1) {
+        const ST ov = __shfl_xor_sync(FULL, val, o);
+        const int oi = __shfl_xor_sync(FULL, idx, o);
+        if (ov > val || (ov == val && oi < idx)) { val = ov; idx = oi; }
+      }
+      const int p = __shfl_sync(FULL, idx, 0);
+      const int src = r == kk ? p : r == p ? kk : r;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) { a[q] = __shfl_sync(FULL, a[q], src); e[q] = __shfl_sync(FULL, e[q], src); }
+      const ST ip = rcp<ST>(__shfl_sync(FULL, a[kk], kk));
+      const ST fct = a[kk];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const ST pa = __shfl_sync(FULL, a[q], kk) * ip, pe = __shfl_sync(FULL, e[q], kk) * ip;
+        if (r == kk) { a[q] = pa; e[q] = pe; }
+        else { a[q] -= fct * pa; e[q] -= fct * pe; }
+      }
+    }
+    if (r < 8) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) W.Hinv[r * 8 + q] = e[q];
     }
   }
   F.is = (ST)(h * rw::gam);
   F.ihc = rcp<ST>((ST)(s - cv[CV_MH]));
   g.sync();
   // rank-2 correction: Z1 = M‚Åª¬π c_Œ¶Ãá, Z2 = M‚Åª¬π c_Œ®
-  solve_M<2>(g, W, M, F, W.Z1, W.Z2);
-  double psi1, rho1, psi2, rho2;
-  functionals(W.Z1, C.w, M, psi1, rho1);
-  functionals(W.Z2, C.w, M, psi2, rho2);
-  const double p1 = phidot(cv, rho1, (double)W.Z1[0], psi1), p2 = phidot(cv, rho2, (double)W.Z2[0], psi2);
-  const double a = 1 - p1, b = -p2, c = -psi1, d = 1 - psi2;
-  const double idet = 1.0 / (a * d - b * c);
+  solve_M<2>(g, W, M, F, scan, W.Z1, W.Z2);
+#pragma unroll
+  for (int sl = 0; sl < NSL; ++sl) {  // head-value terms of the chain back substitutions (own rows)
+    const int i = comp_of<NW>(gt, sl);
+    if (i < M.n && W.att[i] >= 0) { const ST P = W.bP[i]; W.Z1[i] += P * W.Z1[W.att[i]]; W.Z2[i] += P * W.Z2[W.att[i]]; }
+  }
+  ST psi1, p1, psi2, p2;
+  functionals_st(W, W.Z1, M, psi1, p1);
+  functionals_st(W, W.Z2, M, psi2, p2);
+  const ST a = 1 - p1, b = -p2, c = -psi1, d = 1 - psi2;
+  const ST idet = ST(1) / (a * d - b * c);
   F.S00 = d * idet; F.S01 = -b * idet; F.S10 = -c * idet; F.S11 = a * idet;
 }
 
 // W.u = W‚Åª¬π W.r for the thread's own components (W.r complete on entry; W.r is overwritten).
 // Only own slots of W.u are written, so no barrier follows.
 template <int NW, int NSL, typename ST>
-__device__ __forceinline__ void solve_W(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const Factor<ST>& F, const CSet& C,
-                                        const ModelDesc& M) {
-  solve_M<1>(g, W, M, F, W.r, W.r);
-  double psi, rho;
-  functionals(W.r, C.w, M, psi, rho);
-  const double ph = phidot(C.cv, rho, (double)W.r[0], psi);
-  const ST t0 = (ST)(F.S00 * ph + F.S01 * psi), t1 = (ST)(F.S10 * ph + F.S11 * psi);
+__device__ __forceinline__ void solve_W(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const Factor<ST>& F, const ModelDesc& M,
+                                        bool scan) {
+  solve_M<1>(g, W, M, F, scan, W.r, W.r);
+  ST psi, ph;
+  functionals_st(W, W.r, M, psi, ph);
+  const ST t0 = F.S00 * ph + F.S01 * psi, t1 = F.S10 * ph + F.S11 * psi;
 #pragma unroll
   for (int sl = 0; sl < NSL; ++sl) {
-    const int i = g.gt + 32 * NW * sl;
-    if (i < M.n) W.u[i] = W.r[i] + W.Z1[i] * t0 + W.Z2[i] * t1;
+    const int i = comp_of<NW>(g.gt, sl);
+    if (i < M.n) {
+      ST ri = W.r[i];
+      if (W.att[i] >= 0) ri += W.bP[i] * W.r[W.att[i]];  // head-value term of the chain back substitution
+      W.u[i] = ri + W.Z1[i] * t0 + W.Z2[i] * t1;
+    }
   }
 }
 
@@ -492,29 +666,29 @@ __device__ __forceinline__ void solve_W(const Grp<NW>& g, ModeMem<NW, NSL, ST>& 
 template <int NW, int NSL, typename ST>
 __device__ __forceinline__ void stage_solve(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const Factor<ST>& F, const CSet& CJ,
                             const CompDesc* __restrict__ comps, const ModelDesc& M, double k, double s, int refine,
-                            const double (&b)[NSL], double (&U)[NSL]) {
+                            bool scan, const double (&b)[NSL], double (&U)[NSL]) {
   const int gt = g.gt;
 #pragma unroll
-  for (int sl = 0; sl < NSL; ++sl) { const int i = gt + 32 * NW * sl; if (i < M.n) W.r[i] = (ST)b[sl]; }
+  for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) W.r[i] = (ST)b[sl]; }
   g.sync();
-  solve_W(g, W, F, CJ, M);
+  solve_W(g, W, F, M, scan);
 #pragma unroll
-  for (int sl = 0; sl < NSL; ++sl) { const int i = gt + 32 * NW * sl; U[sl] = (i < M.n) ? (double)W.u[i] : 0.0; }
+  for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); U[sl] = (i < M.n) ? (double)W.u[i] : 0.0; }
   for (int it = 0; it < refine; ++it) {
 #pragma unroll
-    for (int sl = 0; sl < NSL; ++sl) { const int i = gt + 32 * NW * sl; if (i < M.n) W.x[i] = U[sl]; }
+    for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) W.x[i] = U[sl]; }
     g.sync();
     double JU[NSL];
     matvec<NW, NSL>(gt, W.x, CJ, comps, M, k, JU);
 #pragma unroll
     for (int sl = 0; sl < NSL; ++sl) {
-      const int i = gt + 32 * NW * sl;
+      const int i = comp_of<NW>(gt, sl);
       if (i < M.n) W.r[i] = (ST)(b[sl] - (s * U[sl] - JU[sl]));
     }
     g.sync();
-    solve_W(g, W, F, CJ, M);
+    solve_W(g, W, F, M, scan);
 #pragma unroll
-    for (int sl = 0; sl < NSL; ++sl) { const int i = gt + 32 * NW * sl; if (i < M.n) U[sl] += (double)W.u[i]; }
+    for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) U[sl] += (double)W.u[i]; }
   }
 }
 
@@ -528,7 +702,7 @@ __device__ void emit_output(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const PtA
   if (A.output == SBZ_OUT_STATE) {
     double* o = A.out + ((size_t)item * A.ntau + j) * M.n;
 #pragma unroll
-    for (int sl = 0; sl < NSL; ++sl) { const int i = gt + 32 * NW * sl; if (i < M.n) o[i] = y[sl]; }
+    for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) o[i] = y[sl]; }
     return;
   }
   if (A.output != SBZ_OUT_SOURCES) return;
@@ -538,13 +712,13 @@ __device__ void emit_output(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const PtA
   coef_eval(g, W, &so, &tau, 1, 1u, true, cd, tab, M.nexpr, M.nx, mk);
   const CSet& CS = W.cs[so];
 #pragma unroll
-  for (int sl = 0; sl < NSL; ++sl) { const int i = gt + 32 * NW * sl; if (i < M.n) W.x[i] = y[sl]; }
+  for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) W.x[i] = y[sl]; }
   g.sync();
   double fy[NSL], dJy[NSL], Jf[NSL], phid, psi, dpsi_w, psi_f;
   matvec<NW, NSL>(gt, W.x, CS, comps, M, k, fy, &phid, &psi);
   matvec_dtau<NW, NSL>(gt, W.x, CS, comps, M, k, dJy, &dpsi_w);
 #pragma unroll
-  for (int sl = 0; sl < NSL; ++sl) { const int i = gt + 32 * NW * sl; if (i < M.n) W.f[i] = fy[sl]; }
+  for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) W.f[i] = fy[sl]; }
   g.sync();
   matvec<NW, NSL>(gt, W.f, CS, comps, M, k, Jf, nullptr, &psi_f);
   if (g.wq == 0) {
@@ -582,6 +756,18 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
   g.sync();
   const double rtol = A.rtol, atol = A.atol;
   const double inv_n = 1.0 / n;
+  bool scan = true;  // every chain fits a warp scan
+  for (int c = 0; c < M.nchain; ++c) scan = scan && (M.chLast[c] - M.chFirst[c] < 32);
+  for (int i = gt; i < NT * NSL; i += NT) {
+    int at = -1;
+    for (int c = 0; c < M.nchain; ++c) if (scan && i >= M.chFirst[c] && i <= M.chLast[c]) at = M.chAttach[c];
+    W.att[i] = (int16_t)at;
+  }
+  if (gt < 8) {
+    int hc = -1;
+    for (int c = 0; c < M.nchain; ++c) if (M.chAttach[c] == 3 + gt) hc = c;
+    W.hatt[gt] = hc;
+  }
 
   for (;;) {
     if (gt == 0) W.item = (int)atomicAdd(A.counter, 1u);
@@ -591,7 +777,13 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
     if (slot >= A.nitems) break;
     const int item = A.order ? A.order[slot] : slot;
     const int c = A.item_cosmo ? A.item_cosmo[item] : 0;
-    const CosmoDesc* cd = A.cosmos + c;
+    {
+      const int* src = reinterpret_cast<const int*>(A.cosmos + c);
+      int* dst = reinterpret_cast<int*>(&W.cdesc);
+      for (int q = gt; q < (int)(sizeof(CosmoDesc) / 4); q += NT) dst[q] = src[q];
+    }
+    g.sync();
+    const CosmoDesc* cd = &W.cdesc;
     const double* tab = A.tables + (size_t)c * A.table_stride;
     const double* taus = A.taus ? A.taus + (size_t)c * A.ntau : nullptr;
     ModeK mk;
@@ -622,7 +814,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
       const double N2 = 2.0 / 15.0 * kt * kt * Psi;
 #pragma unroll
       for (int sl = 0; sl < NSL; ++sl) {
-        const int i = gt + NT * sl;
+        const int i = comp_of<NW>(gt, sl);
         double v = 0;
         if (i < n) {
           if (i == 1 || i == 3) v = -1.5 * Psi;
@@ -676,7 +868,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
     if (t < tend) {
       coef_eval(g, W, &sJ, &t, 1, 1u, false, cd, tab, M.nexpr, M.nx, mk);
 #pragma unroll
-      for (int sl = 0; sl < NSL; ++sl) { const int i = gt + NT * sl; if (i < n) W.x[i] = y[sl]; }
+      for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl]; }
       g.sync();
       matvec<NW, NSL>(gt, W.x, W.cs[sJ], comps, M, k, f0);
       // initial step (Hairer-N√∏rsett-Wanner II.4)
@@ -685,14 +877,14 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         double d0 = 0, d1 = 0;
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) {
-          const int i = gt + NT * sl;
+          const int i = comp_of<NW>(gt, sl);
           if (i < n) { const double sk = atol + fabs(y[sl]) * rtol; d0 += (y[sl] / sk) * (y[sl] / sk); d1 += (f0[sl] / sk) * (f0[sl] / sk); }
         }
         d0 = sqrt(group_sum(g, W, d0) * inv_n); d1 = sqrt(group_sum(g, W, d1) * inv_n);
         double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * d0 / d1;
         h0 = fmin(h0, tend - t);
 #pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) { const int i = gt + NT * sl; if (i < n) W.x[i] = y[sl] + h0 * f0[sl]; }
+        for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl] + h0 * f0[sl]; }
         const double th = t + h0;
         coef_eval(g, W, &s5, &th, 1, 0u, false, cd, tab, M.nexpr, M.nx, mk);
         double f1[NSL];
@@ -700,7 +892,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         double d2 = 0;
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) {
-          const int i = gt + NT * sl;
+          const int i = comp_of<NW>(gt, sl);
           if (i < n) { const double sk = atol + fabs(y[sl]) * rtol; const double q = (f1[sl] - f0[sl]) / (h0 * sk); d2 += q * q; }
         }
         d2 = sqrt(group_sum(g, W, d2) * inv_n);
@@ -709,7 +901,8 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         h = fmin(100 * h0, h1);
         if (!isfinite(h) || h <= 0) h = 1e-6 * fmax(1.0, t);
       }
-      double errold = 1e-4;
+      double errold = 1e-4;   // previous accepted error norm (FP64 controller)
+      float errold2f = 1e-8f; // its square (FP32 controller)
       bool rejected = false, nonfinite = false, have_jac = false;
       Factor<ST> F;
       int64_t iters = 0;
@@ -722,7 +915,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         if (!have_jac) {
           // ‚àÇf/‚àÇœÑ at the step start (J's coefficients are the previous step-end set)
 #pragma unroll
-          for (int sl = 0; sl < NSL; ++sl) { const int i = gt + NT * sl; if (i < n) W.x[i] = y[sl]; }
+          for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl]; }
           g.sync();
           matvec_dtau<NW, NSL>(gt, W.x, CJ, comps, M, k, ft);
           have_jac = true;
@@ -736,41 +929,41 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
           const double tt[4] = {t + rw::c2 * h, t + rw::c3 * h, t + rw::c4 * h, tn};
           g.sync();  // the previous step's readers of these sets are done
           coef_eval(g, W, sets, tt, 4, 8u, false, cd, tab, M.nexpr, M.nx, mk);
-          factorize(g, W, F, CJ, comps, M, k, h, s);
+          factorize(g, W, F, CJ, comps, M, k, h, s, scan);
         }
         double U1[NSL], U2[NSL], U3[NSL], U4[NSL], U5[NSL], U6[NSL], b[NSL], Fv[NSL];
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = f0[sl] + h * rw::d1 * ft[sl];
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, b, U1);
+        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, b, U1);
         // stage 2
 #pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) { const int i = gt + NT * sl; if (i < n) W.x[i] = y[sl] + rw::A21 * U1[sl]; }
+        for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl] + rw::A21 * U1[sl]; }
         g.sync();
         matvec<NW, NSL>(gt, W.x, W.cs[s2], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C21 * U1[sl]) + h * rw::d2 * ft[sl];
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, b, U2);
+        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, b, U2);
         // stage 3
 #pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) { const int i = gt + NT * sl; if (i < n) W.x[i] = y[sl] + rw::A31 * U1[sl] + rw::A32 * U2[sl]; }
+        for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl] + rw::A31 * U1[sl] + rw::A32 * U2[sl]; }
         g.sync();
         matvec<NW, NSL>(gt, W.x, W.cs[s3], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C31 * U1[sl] + rw::C32 * U2[sl]) + h * rw::d3 * ft[sl];
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, b, U3);
+        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, b, U3);
         // stage 4
 #pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) { const int i = gt + NT * sl; if (i < n) W.x[i] = y[sl] + rw::A41 * U1[sl] + rw::A42 * U2[sl] + rw::A43 * U3[sl]; }
+        for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl] + rw::A41 * U1[sl] + rw::A42 * U2[sl] + rw::A43 * U3[sl]; }
         g.sync();
         matvec<NW, NSL>(gt, W.x, W.cs[s4], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C41 * U1[sl] + rw::C42 * U2[sl] + rw::C43 * U3[sl]) + h * rw::d4 * ft[sl];
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, b, U4);
+        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, b, U4);
         // stage 5 (at t + h)
         double Y[NSL];
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) {
-          const int i = gt + NT * sl;
+          const int i = comp_of<NW>(gt, sl);
           Y[sl] = y[sl] + rw::A51 * U1[sl] + rw::A52 * U2[sl] + rw::A53 * U3[sl] + rw::A54 * U4[sl];
           if (i < n) W.x[i] = Y[sl];
         }
@@ -778,28 +971,44 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         matvec<NW, NSL>(gt, W.x, W.cs[s5], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C51 * U1[sl] + rw::C52 * U2[sl] + rw::C53 * U3[sl] + rw::C54 * U4[sl]);
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, b, U5);
+        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, b, U5);
         // stage 6
 #pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) { const int i = gt + NT * sl; Y[sl] += U5[sl]; if (i < n) W.x[i] = Y[sl]; }
+        for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); Y[sl] += U5[sl]; if (i < n) W.x[i] = Y[sl]; }
         g.sync();
         matvec<NW, NSL>(gt, W.x, W.cs[s5], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C61 * U1[sl] + rw::C62 * U2[sl] + rw::C63 * U3[sl] + rw::C64 * U4[sl] + rw::C65 * U5[sl]);
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, b, U6);
-        // error estimate and new state
-        double e2 = 0, y1[NSL];
+        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, b, U6);
+        // error estimate and new state (the norm only steers the step size: FP32 in mixed mode)
+        double y1[NSL], err2;
+        if constexpr (sizeof(ST) == 4) {
+          float e2 = 0;
 #pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) {
-          const int i = gt + NT * sl;
-          y1[sl] = Y[sl] + U6[sl];
-          if (i < n) { const double sk = atol + rtol * fmax(fabs(y[sl]), fabs(y1[sl])); const double q = U6[sl] / sk; e2 += q * q; }
+          for (int sl = 0; sl < NSL; ++sl) {
+            const int i = comp_of<NW>(gt, sl);
+            y1[sl] = Y[sl] + U6[sl];
+            if (i < n) {
+              const float sk = (float)atol + (float)rtol * fmaxf(fabsf((float)y[sl]), fabsf((float)y1[sl]));
+              const float q = __fdividef((float)U6[sl], sk);
+              e2 += q * q;
+            }
+          }
+          err2 = (double)(group_sum(g, W, e2) * (float)inv_n);  // squared RMS error norm
+        } else {
+          double e2 = 0;
+#pragma unroll
+          for (int sl = 0; sl < NSL; ++sl) {
+            const int i = comp_of<NW>(gt, sl);
+            y1[sl] = Y[sl] + U6[sl];
+            if (i < n) { const double sk = atol + rtol * fmax(fabs(y[sl]), fabs(y1[sl])); const double q = U6[sl] / sk; e2 += q * q; }
+          }
+          err2 = group_sum(g, W, e2) * inv_n;
         }
-        const double err2 = group_sum(g, W, e2) * inv_n;  // squared RMS error norm
         if (isfinite(err2) && err2 <= 1.0) {
           // accept: f(t1, y1) with the t1 coefficients, then dense output
 #pragma unroll
-          for (int sl = 0; sl < NSL; ++sl) { const int i = gt + NT * sl; if (i < n) W.x[i] = y1[sl]; }
+          for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y1[sl]; }
           g.sync();
           double f1[NSL];
           matvec<NW, NSL>(gt, W.x, W.cs[s5], comps, M, k, f1);
@@ -823,19 +1032,30 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
 #pragma unroll
           for (int sl = 0; sl < NSL; ++sl) { y[sl] = y1[sl]; f0[sl] = f1[sl]; }
           ++nacc;
-          // PI controller (FP64, as the CPU integrators: the step sequence then follows theirs)
-          const double err = sqrt(err2);
-          double fac = 0.9 * pow(fmax(err, 1e-10), -0.175) * pow(errold, 0.1);
-          fac = fmin(10.0, fmax(0.2, fac));
-          if (rejected) fac = fmin(fac, 1.0);
-          errold = fmax(err, 1e-4);
-          h *= fac;
+          // PI controller fac = 0.9 err^-0.175 errold^0.1: FP32 in mixed mode (a heuristic; FP64 pow
+          // costs ~90 FP64 instructions on this GPU), FP64 as the CPU integrators otherwise
+          if constexpr (sizeof(ST) == 4) {
+            const float e2f = fmaxf((float)err2, 1e-20f);
+            float fac = 0.9f * exp2f(-0.0875f * __log2f(e2f) + 0.05f * __log2f(errold2f));
+            fac = fminf(10.0f, fmaxf(0.2f, fac));
+            if (rejected) fac = fminf(fac, 1.0f);
+            errold2f = fmaxf(e2f, 1e-8f);
+            h *= (double)fac;
+          } else {
+            const double err = sqrt(err2);
+            double fac = 0.9 * pow(fmax(err, 1e-10), -0.175) * pow(errold, 0.1);
+            fac = fmin(10.0, fmax(0.2, fac));
+            if (rejected) fac = fmin(fac, 1.0);
+            errold = fmax(err, 1e-4);
+            h *= fac;
+          }
           rejected = false; nonfinite = false; have_jac = false;
           g.sync();  // x readers are done before the next step writes it
         } else {
           ++nrej;
           rejected = true;
           if (!isfinite(err2)) { nonfinite = true; h *= 0.2; }
+          else if constexpr (sizeof(ST) == 4) h *= (double)fmaxf(0.2f, 0.9f * exp2f(-0.125f * __log2f((float)err2)));
           else h *= fmax(0.2, 0.9 * pow(err2, -0.125));  // 0.9 err^-1/4
           // J's coefficients (at t) and ‚àÇf/‚àÇœÑ stay valid; only the factorisation changes
         }
@@ -850,7 +1070,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
     }
     bool finite = true;
 #pragma unroll
-    for (int sl = 0; sl < NSL; ++sl) { const int i = gt + NT * sl; if (i < n && !isfinite(y[sl])) finite = false; }
+    for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n && !isfinite(y[sl])) finite = false; }
     finite = group_sum(g, W, finite ? 0.0 : 1.0) == 0.0;
     if (status == SBZ_OK && !finite) status = SBZ_NONFINITE;
     if (A.output == SBZ_OUT_DELTA_M) {
@@ -859,7 +1079,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
       g.sync();
       coef_eval(g, W, &so, &tend, 1, 0u, false, cd, tab, M.nexpr, M.nx, mk);
 #pragma unroll
-      for (int sl = 0; sl < NSL; ++sl) { const int i = gt + NT * sl; if (i < n) W.x[i] = y[sl]; }
+      for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl]; }
       g.sync();
       if (g.wq == 0) {
         double I0 = 0, I1 = 0, Ir = 0;

@@ -95,7 +95,7 @@ int build_cosmo(const Background& B, const ModelDesc& M, const sbz_model& m, Cos
   D.lnt0 = B.lnt0; D.idlnt = 1.0 / B.dlnt; D.ntab = B.ntab;
   D.Oc0 = P.Oc0; D.Ob0 = P.Ob0; D.Og0 = P.Og0; D.On0 = P.On0; D.wh = P.wh; D.y0 = P.y0;
   D.R0 = 4.0 / 3.0 * P.Og0 / P.Ob0; D.As = P.As; D.ns = P.ns; D.kpivot = P.kpivot;
-  for (int j = 0; j < M.nx; ++j) { D.xq[j] = P.xq[j]; D.Wq[j] = P.Wq[j]; D.dlnf[j] = P.dlnf[j]; }
+  for (int j = 0; j < M.nx; ++j) { D.xq[j] = P.xq[j]; D.Wq[j] = P.Wq[j]; D.dlnf[j] = P.dlnf[j]; D.ixq[j] = 1.0 / P.xq[j]; }
   int ne = 0;
   auto E = [&](int dest, double K1, int a0, int a1 = B_ONE, int a2 = B_ONE, double K2 = 0, int b0 = B_ONE, int b1 = B_ONE, int b2 = B_ONE) {
     CoefExpr& e = D.expr[ne++];

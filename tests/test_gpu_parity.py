@@ -64,19 +64,33 @@ def test_pk_matches_oracle(S, prob5, bg5, golden):
 
 @pytest.mark.parametrize("tol,bar", [(1e-5, 1e-3), (1e-7, 2e-5)])
 def test_sources_match_oracle(S, prob5, tol, bar):
-    """Line-of-sight sources; differences are at the integrator-tolerance level and shrink with it."""
+    """Line-of-sight sources against the oracle at the same integrator tolerance.
+
+    FP64 mode uses the oracle's arithmetic for the solution and the step-size control, so the two
+    step sequences stay together and the sources agree to well inside the tolerance (bar).  Mixed
+    mode steers the step size in FP32 (the controller is a heuristic), so its step sequence drifts
+    from the oracle's over thousands of steps and the two become independent integrations at the
+    same tolerance.  There the requirement is accuracy parity: the distance to a converged oracle
+    solution (tolerance / 100) is at most three times the oracle's own distance, plus a floor of a
+    tenth of the bar."""
     M = S.ΛCDM(lmax=5)
+    fp64 = prob5.opts.precision == 0
     prob = S.CosmologyProblem(M, S.parameters_Planck18(M), pt_rtol=tol, pt_atol=tol,
-                              precision="fp64" if prob5.opts.precision == 0 else "mixed")
+                              precision="fp64" if fp64 else "mixed")
     bgo = O.Background(O.PLANCK18, MODEL5, pt_rtol=tol, pt_atol=tol)
     ks = np.array([2.0, 50.0, 300.0, 2000.0])
     taus = np.linspace(bgo.tau0 * 0.01, bgo.tau0 * 0.999, 64)
     out, st, _ = S.solvept(prob, ks, 1e-6, saveat=taus, output="sources")
     ref, sto, _ = bgo.solve_pt(ks, 1e-6, taus, mode=0)
-    assert np.all(st == 0) and np.all(sto == 0)
+    conv, stc, _ = O.Background(O.PLANCK18, MODEL5, pt_rtol=tol / 100, pt_atol=tol / 100).solve_pt(ks, 1e-6, taus, mode=0)
+    assert np.all(st == 0) and np.all(sto == 0) and np.all(stc == 0)
     for s in range(3):
-        scale = np.max(np.abs(ref[:, :, s]), axis=1, keepdims=True) + 1e-300
-        assert np.max(np.abs(out[:, :, s] - ref[:, :, s]) / scale) < bar, s
+        scale = np.max(np.abs(conv[:, :, s]), axis=1, keepdims=True) + 1e-300
+        if fp64:
+            assert np.max(np.abs(out[:, :, s] - ref[:, :, s]) / scale) < bar, s
+        ours = np.max(np.abs(out[:, :, s] - conv[:, :, s]) / scale)
+        theirs = np.max(np.abs(ref[:, :, s] - conv[:, :, s]) / scale)
+        assert ours <= 3 * theirs + 0.1 * bar, (s, ours, theirs)
 
 
 def test_state_matches_oracle(S, prob5):
