@@ -173,6 +173,15 @@ def run_ours(args):
             phases.append(t)
             dev_ms.append(t["perturbations"] + t["kinterp"] + t["los"] + t["cl"])
             pt_ms.append(t["perturbations"])
+    # accuracy of the timed configuration (outside the timed region): C_l against an all-FP64 GPU
+    # solve of the same workload; TE relative to sqrt(TT EE)
+    accuracy = None
+    if args.precision == "mixed":
+        p64 = S.CosmologyProblem(M, PARAMS, precision="fp64")
+        Dl64, st64 = S.spectrum_cmb(["TT", "TE", "EE"], p64, jl, lall, kinterp=kinterp, taus=taus, return_status=True)
+        den = [np.abs(Dl64[:, 0]), np.sqrt(np.abs(Dl64[:, 0] * Dl64[:, 2])), np.abs(Dl64[:, 2])]
+        rel = {m: float(np.max(np.abs(Dl[:, i] - Dl64[:, i]) / den[i])) for i, m in enumerate(("TT", "TE", "EE"))}
+        accuracy = {"cl_max_rel_vs_fp64": rel, "l_range": [2, LMAX], "fp64_failed_modes": int(np.count_nonzero(st64))}
     # per-mode step counts for the roofline (one extra solve of the same modes)
     out, stt, stp = S.solvept(prob, ks, prob.opts.tau_ini, saveat=taus, output="sources")
     steps_total = int(stp.sum())
@@ -206,6 +215,7 @@ def run_ours(args):
                      "frac": round(achieved / fp64_peak, 5), "traffic": None,
                      "kernel": "pt_kernel (perturbation modes)", "flops_per_step": fl, "steps_per_launch": steps_total,
                      "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 entry in MEASURED_PEAKS.json)"},
+        "accuracy": accuracy,
         "gpu_launches": int(K * 6),
         "clocks": ck.summary(),
         "hbm_peak_gbs": peaks.get("hbm_gbs"),

@@ -60,10 +60,13 @@ typedef struct sbz_opts {
   double tau_ini, tau_max;  /* background span, default (1e-6, 100) */
   int64_t maxiters;         /* default 100000 */
   int precision;            /* SBZ_FP64 or SBZ_MIXED */
-  int refine_iters;         /* FP64 refinement sweeps per stage solve (SBZ_MIXED), default 1 */
+  int refine_iters;         /* SBZ_MIXED: at most this many FP64 refinement sweeps per stage solve, stopping
+                               once a correction is < 1e-3 of the error tolerance; default 3 */
   int table_points;         /* background coefficient table nodes, default 8192 */
   int warps_per_block;      /* warps per thread block (≤ 4); 0 = 4 */
   int warps_per_mode;       /* warps integrating one mode: 1, 2 or 4; 0 = chosen from the number of modes */
+  int blocks_per_sm;        /* resident thread blocks per SM for the perturbation kernel; 0 = chosen */
+  int los_precision;        /* line of sight: SBZ_FP64 or SBZ_MIXED (FP32 interpolation); -1 = as precision */
 } sbz_opts;
 
 typedef struct sbz_problem sbz_problem;

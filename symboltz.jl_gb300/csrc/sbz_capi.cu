@@ -145,7 +145,8 @@ extern "C" {
 void sbz_default_opts(sbz_opts* o) {
   o->bg_rtol = 1e-7; o->bg_atol = 1e-7; o->pt_rtol = 1e-5; o->pt_atol = 1e-5;
   o->tau_ini = 1e-6; o->tau_max = 100.0; o->maxiters = 100000;
-  o->precision = SBZ_MIXED; o->refine_iters = 1; o->table_points = 8192; o->warps_per_block = 0; o->warps_per_mode = 0;
+  o->precision = SBZ_MIXED; o->refine_iters = 3; o->table_points = 8192; o->warps_per_block = 0; o->warps_per_mode = 0; o->blocks_per_sm = 0;
+  o->los_precision = -1;
 }
 
 const char* sbz_last_error(void) { return g_err.c_str(); }
@@ -337,7 +338,7 @@ static int pt_run(sbz_problem* pb, int nk, const int* d_cosmo, const double* d_k
   A.refine = pb->opts.precision == SBZ_MIXED ? std::max(0, pb->opts.refine_iters) : 0;
   A.counter = pb->d_counter.as<unsigned>();
   SBZ_CUDA(cudaMemsetAsync(A.counter, 0, sizeof(unsigned), pb->stream));
-  const int r = sbz::pt_launch(A, pb->opts.precision, pb->opts.warps_per_block, pb->opts.warps_per_mode, pb->num_sms, pb->stream);
+  const int r = sbz::pt_launch(A, pb->opts.precision, pb->opts.warps_per_block, pb->opts.warps_per_mode, pb->opts.blocks_per_sm, pb->num_sms, pb->stream);
   if (r != SBZ_OK) return fail(r, std::string("perturbation kernel launch: ") + cudaGetErrorString(cudaGetLastError()));
   return SBZ_OK;
 }
@@ -561,7 +562,7 @@ int sbz_spectrum_cmb(sbz_problem* pb, int cosmo, const sbz_bessel* jl, int nc, c
     A.refine = pb->opts.precision == SBZ_MIXED ? std::max(0, pb->opts.refine_iters) : 0;
     A.counter = pb->d_counter.as<unsigned>();
     SBZ_CUDA(cudaMemsetAsync(A.counter, 0, sizeof(unsigned), st));
-    r = sbz::pt_launch(A, pb->opts.precision, pb->opts.warps_per_block, pb->opts.warps_per_mode, pb->num_sms, st);
+    r = sbz::pt_launch(A, pb->opts.precision, pb->opts.warps_per_block, pb->opts.warps_per_mode, pb->opts.blocks_per_sm, pb->num_sms, st);
     if (r != SBZ_OK) return fail(r, "perturbation kernel");
     // the perturbation kernel saves the sources at taus of *this* cosmology: A.taus + cosmo*ntau
   }
@@ -585,7 +586,8 @@ int sbz_spectrum_cmb(sbz_problem* pb, int cosmo, const sbz_bessel* jl, int nc, c
   SBZ_CUDA(pb->c_Th.ensure(sizeof(double) * (size_t)nf * nl * std::max(1, nTE)));
   SBZ_CUDA(pb->c_Thp.ensure(sizeof(double) * (size_t)nf * nl));
   // mixed precision: FP32 interpolation and chunk sums (the C_l target is ~1e-4); FP64 otherwise
-  auto los = pb->opts.precision == SBZ_MIXED && nl <= 1024 ? sbz::los_f32_launch : sbz::los_launch;
+  const int losp = pb->opts.los_precision >= 0 ? pb->opts.los_precision : pb->opts.precision;
+  auto los = losp == SBZ_MIXED && nl <= 1024 ? sbz::los_f32_launch : sbz::los_launch;
   if (nTE > 0 && los(jl->J, const_cast<sbz_bessel*>(jl)->d_ls.as<int>(), nTE, pb->c_Sf.as<double>(), pb->c_taus.as<double>(),
                      pb->c_chi.as<double>(), pb->c_w.as<double>(), ntau, nf, pb->c_ks.as<double>(), nl, pb->c_Th.as<double>(), st) != 0)
     return fail(SBZ_ERR_CUDA, "LOS kernel");

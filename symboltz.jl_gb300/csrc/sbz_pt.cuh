@@ -31,7 +31,8 @@ struct PtArgs {
   unsigned int* counter;      // device work-queue counter, zero before launch
 };
 
-int pt_launch(const PtArgs& A, int precision, int warps_per_block, int warps_per_mode, int num_sms, cudaStream_t stream);
+int pt_launch(const PtArgs& A, int precision, int warps_per_block, int warps_per_mode, int blocks_per_sm, int num_sms,
+              cudaStream_t stream);
 int rhs_launch(const PtArgs& A, const double* y, const double* tau, double* f, double* ft, cudaStream_t st);
 
 }  // namespace sbz

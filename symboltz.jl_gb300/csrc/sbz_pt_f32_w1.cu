@@ -3,17 +3,17 @@
 
 namespace sbz {
 
-int pt_launch_f32_w1(const PtArgs& A, int nw, int warps_per_block, int num_sms, cudaStream_t stream) {
+int pt_launch_f32_w1(const PtArgs& A, int nw, int warps_per_block, int blocks_per_sm, int num_sms, cudaStream_t stream) {
   using namespace ptk;
   switch (nw) {
     case 1:
       switch ((A.model_n + 31) / 32) {
-      case 1: return launch_nw<1, 1, float>(A, warps_per_block, num_sms, stream);
-      case 2: return launch_nw<1, 2, float>(A, warps_per_block, num_sms, stream);
-      case 3: return launch_nw<1, 3, float>(A, warps_per_block, num_sms, stream);
-      case 4: return launch_nw<1, 4, float>(A, warps_per_block, num_sms, stream);
-      case 5: return launch_nw<1, 5, float>(A, warps_per_block, num_sms, stream);
-      case 6: return launch_nw<1, 6, float>(A, warps_per_block, num_sms, stream);
+      case 1: return launch_nw<1, 1, float>(A, warps_per_block, blocks_per_sm, num_sms, stream);
+      case 2: return launch_nw<1, 2, float>(A, warps_per_block, blocks_per_sm, num_sms, stream);
+      case 3: return launch_nw<1, 3, float>(A, warps_per_block, blocks_per_sm, num_sms, stream);
+      case 4: return launch_nw<1, 4, float>(A, warps_per_block, blocks_per_sm, num_sms, stream);
+      case 5: return launch_nw<1, 5, float>(A, warps_per_block, blocks_per_sm, num_sms, stream);
+      case 6: return launch_nw<1, 6, float>(A, warps_per_block, blocks_per_sm, num_sms, stream);
         default: return SBZ_ERR_ARG;
       }
     default: return SBZ_ERR_ARG;

@@ -133,6 +133,24 @@ __device__ __forceinline__ T group_sum(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W
   }
 }
 
+template <int NW, int NSL, typename ST>
+__device__ __forceinline__ float group_max(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, float v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(FULL, v, o));
+  if constexpr (NW == 1) {
+    __syncwarp();
+    return v;
+  } else {
+    if (g.lane == 0) W.red[g.rp][g.wq] = v;
+    g.sync();
+    float s = 0;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) s = fmaxf(s, (float)W.red[g.rp][w]);
+    g.rp ^= 1;
+    return s;
+  }
+}
+
 template <typename ST>
 __device__ __forceinline__ ST rcp(ST v);
 template <>
@@ -661,12 +679,16 @@ __device__ __forceinline__ void solve_W(const Grp<NW>& g, ModeMem<NW, NSL, ST>& 
   }
 }
 
-// U = W⁻¹ b with optional FP64 iterative refinement (W = s I - J at the step start).
-// W.r and W.x must be free (no thread still reading them) on entry.
+// U = W⁻¹ b with FP64 iterative refinement (W = s I - J at the step start): up to `refine`
+// corrections, stopping once the largest correction is below 1e-3 in units of the integrator's
+// error weights (isk = 1/(atol + rtol |y|)).  In the stiff tight-coupling era the FP32 head solve
+// has condition number ~κ̇h and one correction leaves a bias that accumulates over the steps;
+// elsewhere one correction is enough.  W.r and W.x must be free (no thread still reading them) on
+// entry.
 template <int NW, int NSL, typename ST>
 __device__ __forceinline__ void stage_solve(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const Factor<ST>& F, const CSet& CJ,
                             const CompDesc* __restrict__ comps, const ModelDesc& M, double k, double s, int refine,
-                            bool scan, const double (&b)[NSL], double (&U)[NSL]) {
+                            bool scan, const float (&isk)[NSL], const double (&b)[NSL], double (&U)[NSL]) {
   const int gt = g.gt;
 #pragma unroll
   for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) W.r[i] = (ST)b[sl]; }
@@ -687,8 +709,13 @@ __device__ __forceinline__ void stage_solve(const Grp<NW>& g, ModeMem<NW, NSL, S
     }
     g.sync();
     solve_W(g, W, F, M, scan);
+    float c = 0.0f;
 #pragma unroll
-    for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) U[sl] += (double)W.u[i]; }
+    for (int sl = 0; sl < NSL; ++sl) {
+      const int i = comp_of<NW>(gt, sl);
+      if (i < M.n) { const ST d = W.u[i]; U[sl] += (double)d; c = fmaxf(c, fabsf((float)d) * isk[sl]); }
+    }
+    if (it + 1 < refine && group_max(g, W, c) < 1e-3f) break;
   }
 }
 
@@ -932,9 +959,12 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
           factorize(g, W, F, CJ, comps, M, k, h, s, scan);
         }
         double U1[NSL], U2[NSL], U3[NSL], U4[NSL], U5[NSL], U6[NSL], b[NSL], Fv[NSL];
+        float isk[NSL];  // refinement stopping weights
+#pragma unroll
+        for (int sl = 0; sl < NSL; ++sl) isk[sl] = 1.0f / (float)(atol + rtol * fabs(y[sl]));
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = f0[sl] + h * rw::d1 * ft[sl];
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, b, U1);
+        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, isk, b, U1);
         // stage 2
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl] + rw::A21 * U1[sl]; }
@@ -942,7 +972,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         matvec<NW, NSL>(gt, W.x, W.cs[s2], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C21 * U1[sl]) + h * rw::d2 * ft[sl];
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, b, U2);
+        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, isk, b, U2);
         // stage 3
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl] + rw::A31 * U1[sl] + rw::A32 * U2[sl]; }
@@ -950,7 +980,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         matvec<NW, NSL>(gt, W.x, W.cs[s3], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C31 * U1[sl] + rw::C32 * U2[sl]) + h * rw::d3 * ft[sl];
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, b, U3);
+        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, isk, b, U3);
         // stage 4
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl] + rw::A41 * U1[sl] + rw::A42 * U2[sl] + rw::A43 * U3[sl]; }
@@ -958,7 +988,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         matvec<NW, NSL>(gt, W.x, W.cs[s4], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C41 * U1[sl] + rw::C42 * U2[sl] + rw::C43 * U3[sl]) + h * rw::d4 * ft[sl];
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, b, U4);
+        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, isk, b, U4);
         // stage 5 (at t + h)
         double Y[NSL];
 #pragma unroll
@@ -971,7 +1001,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         matvec<NW, NSL>(gt, W.x, W.cs[s5], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C51 * U1[sl] + rw::C52 * U2[sl] + rw::C53 * U3[sl] + rw::C54 * U4[sl]);
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, b, U5);
+        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, isk, b, U5);
         // stage 6
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); Y[sl] += U5[sl]; if (i < n) W.x[i] = Y[sl]; }
@@ -979,7 +1009,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         matvec<NW, NSL>(gt, W.x, W.cs[s5], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C61 * U1[sl] + rw::C62 * U2[sl] + rw::C63 * U3[sl] + rw::C64 * U4[sl] + rw::C65 * U5[sl]);
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, b, U6);
+        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, isk, b, U6);
         // error estimate and new state (the norm only steers the step size: FP32 in mixed mode)
         double y1[NSL], err2;
         if constexpr (sizeof(ST) == 4) {
@@ -1131,7 +1161,7 @@ __global__ void __launch_bounds__(128) pt_kernel(PtArgs A) {
 }
 
 template <int NW, int NSL, typename ST>
-int launch_nw(const PtArgs& A, int warps_per_block, int num_sms, cudaStream_t stream) {
+int launch_nw(const PtArgs& A, int warps_per_block, int blocks_per_sm, int num_sms, cudaStream_t stream) {
   using Mem = ModeMem<NW, NSL, ST>;
   const int wpb = warps_per_block < NW ? NW : warps_per_block > 4 ? 4 : warps_per_block;  // ≤ 128 threads
   const int groups = wpb / NW;
@@ -1142,6 +1172,7 @@ int launch_nw(const PtArgs& A, int warps_per_block, int num_sms, cudaStream_t st
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * NW * groups, smem) != cudaSuccess) return SBZ_ERR_CUDA;
   per_sm = per_sm < 1 ? 1 : per_sm;
+  if (blocks_per_sm > 0 && blocks_per_sm < per_sm) per_sm = blocks_per_sm;
   const int want = (A.nitems + groups - 1) / groups;
   const int grid = want < num_sms * per_sm ? want : num_sms * per_sm;
   kern<<<grid > 0 ? grid : 1, 32 * NW * groups, smem, stream>>>(A);

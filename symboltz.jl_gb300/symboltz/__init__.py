@@ -99,8 +99,8 @@ class CosmologyProblem:
     all of them share the model and are solved together (one kernel launch for all their modes)."""
 
     def __init__(self, M: Model, pars, *, bg_rtol=1e-7, bg_atol=1e-7, pt_rtol=1e-5, pt_atol=1e-5, ivspan=(1e-6, 100.0),
-                 maxiters=100000, precision="mixed", refine_iters=1, table_points=8192, warps_per_block=0,
-                 warps_per_mode=0):
+                 maxiters=100000, precision="mixed", refine_iters=3, table_points=8192, warps_per_block=0,
+                 warps_per_mode=0, blocks_per_sm=0, los_precision=None):
         self.M = M
         self.pars = [dict(p) for p in ([pars] if isinstance(pars, dict) else pars)]
         o = L.Opts()
@@ -110,7 +110,8 @@ class CosmologyProblem:
         o.maxiters = maxiters
         o.precision = {"mixed": L.SBZ_MIXED, "fp64": L.SBZ_FP64}[precision]
         o.refine_iters, o.table_points, o.warps_per_block = refine_iters, table_points, warps_per_block
-        o.warps_per_mode = warps_per_mode
+        o.warps_per_mode, o.blocks_per_sm = warps_per_mode, blocks_per_sm
+        o.los_precision = -1 if los_precision is None else {"fp64": L.SBZ_FP64, "mixed": L.SBZ_MIXED}[los_precision]
         self.opts = o
         self._m = M.c()
         pc, n = _params_c(self.pars)
