@@ -46,16 +46,15 @@ def workload_grids(S, prob):
 
 
 def fp64_flops_per_step(n, refine):
-    """FP64-equivalent flops of one Rodas4 step of the implemented structured algorithm
-    (2 flops per FMA): 7 operator evaluations, ∂f/∂τ, factorisation (chains, 8x8 head LU, two
-    rank-2 solves), 6 stage solves (+ refinement: one operator product and one solve each),
-    stage combinations, error norm."""
-    F_mv = 12 * n
-    F_solve = 12 * n + 128
-    F_ft = 16 * n
-    F_fac = 6 * n + 680 + 2 * F_solve
-    f = 7 * F_mv + F_ft + F_fac + 6 * F_solve + 58 * n + 8 * n
-    f += refine * 6 * (F_mv + F_solve + 4 * n)
+    """FP64 flops of one Rodas4 step as implemented (2 flops per FMA), counting only the work done
+    in FP64: 7 operator products (11 flops per row + 60 for the metric functionals), ∂f/∂τ,
+    `refine` residual products per stage (operator product + 2 per row), the stage combinations
+    (58 per row), the factorisation inputs (4 per row) and the coefficient sets (~3.2k).  In mixed
+    precision the stage solves, factorisation, error norm and step control are FP32 and not counted;
+    refine = 1 is the minimum of the adaptive refinement."""
+    F_mv = 11 * n + 60
+    f = 7 * F_mv + (15 * n + 100) + 58 * n + 4 * n + 3240
+    f += refine * 6 * (F_mv + 2 * n)
     return f
 
 
@@ -180,8 +179,14 @@ def run_ours(args):
         p64 = S.CosmologyProblem(M, PARAMS, precision="fp64")
         Dl64, st64 = S.spectrum_cmb(["TT", "TE", "EE"], p64, jl, lall, kinterp=kinterp, taus=taus, return_status=True)
         den = [np.abs(Dl64[:, 0]), np.sqrt(np.abs(Dl64[:, 0] * Dl64[:, 2])), np.abs(Dl64[:, 2])]
-        rel = {m: float(np.max(np.abs(Dl[:, i] - Dl64[:, i]) / den[i])) for i, m in enumerate(("TT", "TE", "EE"))}
-        accuracy = {"cl_max_rel_vs_fp64": rel, "l_range": [2, LMAX], "fp64_failed_modes": int(np.count_nonzero(st64))}
+        accuracy = {"reference": "all-FP64 GPU solve, same tolerances and grids", "fp64_failed_modes": int(np.count_nonzero(st64))}
+        for lo, hi in ((2, LMAX), (2, 29), (30, LMAX)):
+            sel = (lall >= lo) & (lall <= hi)
+            rel = {}
+            for i, m in enumerate(("TT", "TE", "EE")):
+                r = np.abs(Dl[sel, i] - Dl64[sel, i]) / den[i][sel]
+                rel[m] = {"max": float(r.max()), "at_l": int(lall[sel][np.argmax(r)]), "median": float(np.median(r))}
+            accuracy[f"cl_rel_l{lo}_{hi}"] = rel
     # per-mode step counts for the roofline (one extra solve of the same modes)
     out, stt, stp = S.solvept(prob, ks, prob.opts.tau_ini, saveat=taus, output="sources")
     steps_total = int(stp.sum())
@@ -192,6 +197,8 @@ def run_ours(args):
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         dev, e2e = tt.tolist()
     K = args.steps
+    tau0 = float(prob.solvebg().tau0[0])
+    nk_fine = int(len(S.lingrid(float(ks.min()), float(ks.max()), step=np.pi / tau0)))
     value = world * NK * K / (dev / 1e3)
     e2e_v = world * NK * K / (e2e / 1e3)
     peaks = measured_peaks()
@@ -205,7 +212,7 @@ def run_ours(args):
         "dtype": "f64" if args.precision == "fp64" else "f64+f32",
         "data": "synthetic (fixed cosmological parameters)",
         "config": {"workload": "LCDM+massive-nu, l_gamma=30, 1000 k log 1e-5..5 h/Mpc, 2000 tau, TT/TE/EE to l=2500",
-                   "n_state": prob.nstate, "nk": NK, "ntau": NTAU, "nl_sampled": int(len(ls)), "nk_fine": None,
+                   "n_state": prob.nstate, "nk": NK, "ntau": NTAU, "nl_sampled": int(len(ls)), "nk_fine": nk_fine,
                    "precision": args.precision, "pt_rtol": prob.opts.pt_rtol, "l2": "flushed (256 MB write) between steps"},
         "cosmologies_per_s": round(world * K / (dev / 1e3), 4),
         "e2e": {"value": round(e2e_v, 2), "unit": "k-modes/s", "cosmologies_per_s": round(world * K / (e2e / 1e3), 4),
@@ -279,13 +286,22 @@ def run_reference(args):
 
 
 def profile_case(args):
+    """Small cases for ncu section captures.  pt: 64 of the 1000 modes (even in log k, the slowest
+    included), sources on 200 times.  los: one spectrum_cmb of the full workload (the line-of-sight
+    kernel runs once on the full fine k grid; ~1.5 GB on the device)."""
     import symboltz as S
     M = S.ΛCDM(lmax_gamma=MODEL["lmax_gamma"], lmax_nu=MODEL["lmax_nu"], lmax_h=MODEL["lmax_h"], nx=MODEL["nx"])
     prob = S.CosmologyProblem(M, PARAMS, precision=args.precision)
     ks, taus, ls = workload_grids(S, prob)
-    sel = ks[np.linspace(0, len(ks) - 1, 64).round().astype(int)]
-    out, st, stp = S.solvept(prob, sel, prob.opts.tau_ini, saveat=taus[::10], output="sources")
-    print(json.dumps({"profile_case": "64 modes, 200 saved times", "failed": int(np.count_nonzero(st)), "steps": int(stp.sum())}))
+    if args.profile_case == "pt":
+        sel = ks[np.linspace(0, len(ks) - 1, 64).round().astype(int)]
+        out, st, stp = S.solvept(prob, sel, prob.opts.tau_ini, saveat=taus[::10], output="sources")
+        print(json.dumps({"profile_case": "pt: 64 modes, 200 saved times", "failed": int(np.count_nonzero(st)), "steps": int(stp.sum())}))
+    else:
+        jl = S.SphericalBesselCache(ls)
+        Dl, st = S.spectrum_cmb(["TT", "TE", "EE"], prob, jl, np.arange(2, LMAX + 1), kinterp=S.CubicSplineInterpolator(ks, f=np.log),
+                                taus=taus, return_status=True)
+        print(json.dumps({"profile_case": "los: one spectrum_cmb", "failed": int(np.count_nonzero(st)), "timings_ms": S.timings(prob)}))
 
 
 def main():
@@ -297,8 +313,8 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile-case", action="store_true",
-                    help="small case for ncu section captures: 64 of the 1000 modes, 200 saved times")
+    ap.add_argument("--profile-case", choices=("pt", "los"), default=None,
+                    help="small cases for ncu section captures (see profile_case)")
     args = ap.parse_args()
     if args.profile_case:
         profile_case(args)
