@@ -285,6 +285,67 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def batched_workload(ncosmo=256, seed=0):
+    """256 cosmologies drawn uniformly from the parameter box (numpy PCG64, fixed seed): h in
+    [0.6, 0.8], ω_c in [0.10, 0.14], ω_b in [0.020, 0.024], n_s in [0.92, 1.0], ln(1e10 A_s) in
+    [2.9, 3.2], Σm_ν in [0.06, 0.3] eV (one massive species of that mass); each with its own
+    log-spaced k grid of U{200..800} modes over 1e-5..5 h/Mpc."""
+    rng = np.random.default_rng(seed)
+    pars = []
+    for _ in range(ncosmo):
+        h = rng.uniform(0.6, 0.8)
+        oc, ob = rng.uniform(0.10, 0.14), rng.uniform(0.020, 0.024)
+        ns, las, mnu = rng.uniform(0.92, 1.0), rng.uniform(2.9, 3.2), rng.uniform(0.06, 0.3)
+        pars.append(dict(h=h, Omega_c=oc / h**2, Omega_b=ob / h**2, T0=2.7255, Neff=2.0328, YHe=0.245, ln_As1e10=las, ns=ns,
+                         m_nu_eV=mnu, N_nu=1.0))
+    nks = rng.integers(200, 801, size=ncosmo)
+    return pars, nks
+
+
+def run_batched(args):
+    """Batched P(k): every mode of every cosmology in one perturbation launch (Δm output), the
+    launch shape picked by the autotuner, mixed precision against all-FP64."""
+    import torch
+    import symboltz as S
+    assert torch.cuda.is_available(), "bench needs a GPU"
+    pars, nks = batched_workload()
+    M = S.ΛCDM(lmax_gamma=MODEL["lmax_gamma"], lmax_nu=MODEL["lmax_nu"], lmax_h=MODEL["lmax_h"], nx=MODEL["nx"])
+    ks = np.concatenate([S.k_from_hMpc(S.loggrid(1e-5, 5.0, length=int(n))) for n in nks])
+    cos = np.concatenate([np.full(int(n), i) for i, n in enumerate(nks)])
+    ti = lambda k: np.minimum(1e-2 / k, 1e-4)  # noqa: E731  (spectrum_matter's rule, fourier.jl:76-81)
+    res, chosen = {}, {}
+    for prec in ("mixed", "fp64"):  # the FP64 run uses the launch shape tuned for the mixed run
+        prob = S.CosmologyProblem(M, pars, precision=prec, **chosen)
+        t0 = time.perf_counter()
+        bg = prob.solvebg()
+        t_bg = time.perf_counter() - t0
+        assert np.all(bg.status == 0)
+        tune = None
+        if prec == "mixed":
+            tune = S.autotune(prob, ks, ti, output="delta_m", cosmo=cos)
+            chosen = dict(warps_per_mode=tune["warps_per_mode"], blocks_per_sm=tune["blocks_per_sm"])
+        times = []
+        for _ in range(max(1, args.steps)):
+            t0 = time.perf_counter()
+            dm, st, stp = S.solvept(prob, ks, ti, output="delta_m", cosmo=cos)
+            times.append(time.perf_counter() - t0)
+        res[prec] = dict(s=min(times), dm=dm, failed=int(np.count_nonzero(st)), steps=int(stp.sum()), bg_s=t_bg, tune=tune)
+    rel = np.abs(res["mixed"]["dm"] ** 2 - res["fp64"]["dm"] ** 2) / res["fp64"]["dm"] ** 2
+    n = len(ks)
+    line = {"metric": "k-mode solves/s (batched P(k))", "value": round(n / res["mixed"]["s"], 2), "unit": "k-modes/s",
+            "workload": f"batched: {len(pars)} cosmologies from the parameter box, U{{200..800}} k each ({n} modes), P(k) at z=0",
+            "config": {"model": "LCDM+massive-nu, l_gamma=30, n_state=133", "seed": 0, "launches": 1},
+            "mixed": {"s": round(res["mixed"]["s"], 3), "kmodes_per_s": round(n / res["mixed"]["s"], 1), "failed": res["mixed"]["failed"],
+                      "steps": res["mixed"]["steps"], "autotune": {"chosen": [res["mixed"]["tune"]["warps_per_mode"], res["mixed"]["tune"]["blocks_per_sm"]],
+                                                                   "candidates_ms": {str(k): round(v, 1) for k, v in res["mixed"]["tune"]["candidates_ms"].items()}}},
+            "fp64": {"s": round(res["fp64"]["s"], 3), "kmodes_per_s": round(n / res["fp64"]["s"], 1), "failed": res["fp64"]["failed"],
+                     "steps": res["fp64"]["steps"]},
+            "speedup_mixed_over_fp64": round(res["fp64"]["s"] / res["mixed"]["s"], 3),
+            "pk_rel_mixed_vs_fp64": {"max": float(rel.max()), "median": float(np.median(rel))},
+            "background_s": round(res["mixed"]["bg_s"], 3)}
+    print(json.dumps(line), flush=True)
+
+
 def profile_case(args):
     """Small cases for ncu section captures.  pt: 64 of the 1000 modes (even in log k, the slowest
     included), sources on 200 times.  los: one spectrum_cmb of the full workload (the line-of-sight
@@ -313,11 +374,15 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=("spectrum", "batched"), default="spectrum",
+                    help="spectrum: the headline single-cosmology C_l workload; batched: 256 cosmologies, ragged k grids")
     ap.add_argument("--profile-case", choices=("pt", "los"), default=None,
                     help="small cases for ncu section captures (see profile_case)")
     args = ap.parse_args()
     if args.profile_case:
         profile_case(args)
+    elif args.workload == "batched" and args.impl == "ours":
+        run_batched(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

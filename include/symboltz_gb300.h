@@ -157,6 +157,16 @@ int sbz_problem_set_stream(sbz_problem* pb, void* stream);
  * line of sight, C_l, D2H, total, (reserved). */
 int sbz_problem_timings(const sbz_problem* pb, double* ms8);
 
+/* No counterpart in the reference (its solvept threads over k on the CPU).  Autotuner for the
+ * perturbation kernel's launch shape: times the candidates (warps per mode, blocks per SM) =
+ * (1,0) (2,0) (2,2) (4,1) (4,2) (4,3) on a k-stratified sample of the given modes (an eighth of
+ * them above 2048 modes, all of them otherwise), stores the fastest in the problem's options and
+ * returns it in best[2]; ms[SBZ_TUNE_CANDIDATES] receives the candidates' kernel times (may be
+ * NULL).  Arguments as sbz_solve_pt. */
+#define SBZ_TUNE_CANDIDATES 6
+int sbz_autotune_pt(sbz_problem* pb, int nk, const int* cosmo, const double* ks, const double* tau_ini, int ntau,
+                    const double* taus, int output, int* best, double* ms);
+
 /* spectrum_cmb(ΘlAs, ΘlBs, P0s, ls, ks) (src/observables/angular.jl:198-223): natural cubic
  * spline through (0,0) and (k, 2/π k² P0 Θ_A Θ_B), integrated exactly.  Th[ik*nl + il]. */
 int sbz_cl_integrate(int nk, const double* ks, const double* P0, int nl, const double* ThA,

@@ -432,6 +432,67 @@ int sbz_solve_pt(sbz_problem* pb, int nk, const int* cosmo, const double* ks, co
   return SBZ_OK;
 }
 
+int sbz_autotune_pt(sbz_problem* pb, int nk, const int* cosmo, const double* ks, const double* tau_ini, int ntau,
+                    const double* taus, int output, int* best, double* ms) {
+  if (!check_pt_args(pb, nk, ntau, output)) return SBZ_ERR_ARG;
+  if (nk <= 0 || !ks || !tau_ini) return fail(SBZ_ERR_ARG, "sbz_autotune_pt: bad arguments");
+  // stratified sample in k (every m-th mode of the k-sorted list): large batches are timed on an
+  // eighth of their modes, small ones in full, so the sample stays in the same regime (tail-bound
+  // or throughput-bound) as the workload
+  std::vector<int> byk(nk);
+  std::iota(byk.begin(), byk.end(), 0);
+  std::stable_sort(byk.begin(), byk.end(), [&](int a, int b) { return ks[a] > ks[b]; });
+  const int m = nk > 2048 ? 8 : 1;
+  std::vector<int> sc, order;
+  std::vector<double> sk, st;
+  for (int i = 0; i < nk; i += m) {
+    const int j = byk[i];
+    const int c = cosmo ? cosmo[j] : 0;
+    if (c < 0 || c >= pb->ncosmo) return fail(SBZ_ERR_ARG, "cosmology index out of range");
+    sk.push_back(ks[j]); st.push_back(tau_ini[j]); sc.push_back(c); order.push_back((int)order.size());
+  }
+  const int ns = (int)sk.size(), n = pb->M.n;
+  const size_t nout = output == SBZ_OUT_DELTA_M ? (size_t)ns : output == SBZ_OUT_SOURCES ? (size_t)ns * ntau * 3 : (size_t)ns * ntau * n;
+  cudaStream_t s = pb->stream;
+  SBZ_CUDA(pb->d_k.ensure(sizeof(double) * ns));
+  SBZ_CUDA(pb->d_ti.ensure(sizeof(double) * ns));
+  SBZ_CUDA(pb->d_cosmo.ensure(sizeof(int) * ns));
+  SBZ_CUDA(pb->d_order.ensure(sizeof(int) * ns));
+  SBZ_CUDA(pb->d_taus.ensure(sizeof(double) * std::max<size_t>(1, (size_t)ntau * pb->ncosmo)));
+  SBZ_CUDA(pb->d_out.ensure(sizeof(double) * nout));
+  SBZ_CUDA(pb->d_status.ensure(sizeof(int) * ns));
+  SBZ_CUDA(pb->d_steps.ensure(sizeof(int64_t) * 2 * ns));
+  SBZ_CUDA(cudaMemcpyAsync(pb->d_k.p, sk.data(), sizeof(double) * ns, cudaMemcpyHostToDevice, s));
+  SBZ_CUDA(cudaMemcpyAsync(pb->d_ti.p, st.data(), sizeof(double) * ns, cudaMemcpyHostToDevice, s));
+  SBZ_CUDA(cudaMemcpyAsync(pb->d_cosmo.p, sc.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s));
+  SBZ_CUDA(cudaMemcpyAsync(pb->d_order.p, order.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s));
+  if (ntau > 0) SBZ_CUDA(cudaMemcpyAsync(pb->d_taus.p, taus, sizeof(double) * ntau * pb->ncosmo, cudaMemcpyHostToDevice, s));
+  int r;
+  if ((r = ensure_events(pb)) != SBZ_OK) return r;
+  const int cand[SBZ_TUNE_CANDIDATES][2] = {{1, 0}, {2, 0}, {2, 2}, {4, 1}, {4, 2}, {4, 3}};
+  const int keep_nw = pb->opts.warps_per_mode, keep_bps = pb->opts.blocks_per_sm;
+  double best_ms = 1e300;
+  int bi = 0;
+  for (int c = 0; c < SBZ_TUNE_CANDIDATES; ++c) {
+    pb->opts.warps_per_mode = cand[c][0];
+    pb->opts.blocks_per_sm = cand[c][1];
+    SBZ_CUDA(cudaEventRecord(pb->ev[8], s));
+    r = pt_run(pb, ns, pb->d_cosmo.as<int>(), pb->d_k.as<double>(), pb->d_ti.as<double>(), pb->d_order.as<int>(), ntau,
+               pb->d_taus.as<double>(), output, pb->d_out.as<double>(), pb->d_status.as<int>(), pb->d_steps.as<int64_t>());
+    if (r != SBZ_OK) { pb->opts.warps_per_mode = keep_nw; pb->opts.blocks_per_sm = keep_bps; return r; }
+    SBZ_CUDA(cudaEventRecord(pb->ev[9], s));
+    SBZ_CUDA(cudaEventSynchronize(pb->ev[9]));
+    float t = 0;
+    cudaEventElapsedTime(&t, pb->ev[8], pb->ev[9]);
+    if (ms) ms[c] = t;
+    if (t < best_ms) { best_ms = t; bi = c; }
+  }
+  pb->opts.warps_per_mode = cand[bi][0];
+  pb->opts.blocks_per_sm = cand[bi][1];
+  if (best) { best[0] = cand[bi][0]; best[1] = cand[bi][1]; }
+  return SBZ_OK;
+}
+
 int sbz_spectrum_primordial(const sbz_problem* pb, int cosmo, int nk, const double* ks, double* P0) {
   if (!pb || cosmo < 0 || cosmo >= pb->ncosmo) return fail(SBZ_ERR_ARG, "bad cosmology");
   sbz::Cosmo P;

@@ -178,6 +178,33 @@ def solvebg(prob: CosmologyProblem):
 _OUT = {"sources": L.SBZ_OUT_SOURCES, "delta_m": L.SBZ_OUT_DELTA_M, "state": L.SBZ_OUT_STATE}
 
 
+def autotune(prob: CosmologyProblem, ks, ptivini=-np.inf, *, saveat=None, output="sources", cosmo=None):
+    """Pick the perturbation kernel's launch shape (warps per mode, blocks per SM) for this workload
+    by timing the candidates on a k-stratified sample of it (``sbz_autotune_pt``); the choice is
+    stored in the problem and used by later solves.  Returns {"warps_per_mode", "blocks_per_sm",
+    "candidates_ms": {(nw, bps): ms}}."""
+    prob.solvebg()
+    ks = L.f64(np.atleast_1d(ks))
+    nk = len(ks)
+    ti = np.asarray(ptivini(ks) if callable(ptivini) else np.full(nk, ptivini), dtype=np.float64)
+    ti = L.f64(np.broadcast_to(ti, (nk,)))
+    cos = L.i32(np.zeros(nk) if cosmo is None else cosmo)
+    kind = _OUT[output]
+    if kind == L.SBZ_OUT_DELTA_M:
+        taus = np.zeros((prob.ncosmo, 0))
+    else:
+        taus = np.asarray(saveat, dtype=np.float64)
+        taus = np.broadcast_to(taus, (prob.ncosmo, taus.shape[-1])) if taus.ndim == 1 else taus
+    taus = L.f64(taus)
+    best = L.i32(np.zeros(2))
+    ms = L.f64(np.zeros(6))
+    L.check(L.lib().sbz_autotune_pt(prob._h, nk, L.iptr(cos), L.dptr(ks), L.dptr(ti), taus.shape[1], L.dptr(taus), kind,
+                                    L.iptr(best), L.dptr(ms)), "autotune")
+    cands = [(1, 0), (2, 0), (2, 2), (4, 1), (4, 2), (4, 3)]
+    prob.opts.warps_per_mode, prob.opts.blocks_per_sm = int(best[0]), int(best[1])
+    return {"warps_per_mode": int(best[0]), "blocks_per_sm": int(best[1]), "candidates_ms": {c: float(m) for c, m in zip(cands, ms)}}
+
+
 def solvept(prob: CosmologyProblem, ks, ptivini=-np.inf, *, saveat=None, output="state", cosmo=None):
     """solvept (src/solve.jl:543-569) for modes ks (cosmology index per mode in ``cosmo``).
 

@@ -188,3 +188,38 @@ def test_rhs_matches_oracle(S, prob5, bg5):
             np.testing.assert_array_less(np.abs(f[i, idx] - fo) / scale, 1e-6, err_msg=f"f tau={tau} k={k}")
             tscale = np.abs(fto).max() + 1e-300
             assert np.max(np.abs(ft[i, idx] - fto)) / tscale < 1e-3, (tau, k)
+
+
+def test_batched_cosmologies_match_single_solves(S):
+    """Several cosmologies with ragged k grids in one launch give, mode for mode, the same Δm as
+    each cosmology solved alone (modes are independent; same launch shape → same arithmetic)."""
+    M = S.ΛCDM(lmax=5)
+    base = S.parameters_Planck18(M)
+    pars = [dict(base, h=0.62 + 0.04 * i, Omega_c=base["Omega_c"] * (0.9 + 0.1 * i)) for i in range(3)]
+    rng = np.random.default_rng(0)
+    nks = rng.integers(8, 24, size=3)
+    ks = [S.k_from_hMpc(S.loggrid(1e-4, 2.0, length=int(n))) for n in nks]
+    cos = np.concatenate([np.full(int(n), i) for i, n in enumerate(nks)])
+    ti = lambda k: np.minimum(1e-2 / k, 1e-4)  # noqa: E731
+    batch = S.CosmologyProblem(M, pars, warps_per_mode=4)
+    dm, st, _ = S.solvept(batch, np.concatenate(ks), ti, output="delta_m", cosmo=cos)
+    assert np.all(st == 0)
+    for i, p in enumerate(pars):
+        one = S.CosmologyProblem(M, p, warps_per_mode=4)
+        d1, s1, _ = S.solvept(one, ks[i], ti, output="delta_m")
+        assert np.all(s1 == 0)
+        np.testing.assert_array_equal(dm[cos == i], d1)
+
+
+def test_autotune_picks_a_candidate_and_keeps_results(S):
+    M = S.ΛCDM(lmax=5)
+    prob = S.CosmologyProblem(M, S.parameters_Planck18(M))
+    ks = S.k_from_hMpc(S.loggrid(1e-4, 1.0, length=40))
+    ti = lambda k: np.minimum(1e-2 / k, 1e-4)  # noqa: E731
+    ref, _, _ = S.solvept(prob, ks, ti, output="delta_m")
+    tune = S.autotune(prob, ks, ti, output="delta_m")
+    assert (tune["warps_per_mode"], tune["blocks_per_sm"]) in tune["candidates_ms"]
+    assert all(v > 0 for v in tune["candidates_ms"].values())
+    got, st, _ = S.solvept(prob, ks, ti, output="delta_m")
+    assert np.all(st == 0)
+    np.testing.assert_allclose(got, ref, rtol=1e-4)  # another launch shape: same solution to tolerance
