@@ -167,6 +167,22 @@ int sbz_problem_timings(const sbz_problem* pb, double* ms8);
 int sbz_autotune_pt(sbz_problem* pb, int nk, const int* cosmo, const double* ks, const double* tau_ini, int ntau,
                     const double* taus, int output, int* best, double* ms);
 
+/* No counterpart in the reference: the source surrogate's dense-layer GEMM (BF16 tcgen05 tensor
+ * cores, FP32 accumulation), exposed for testing.  D = A·Bᵀ with A [M][K] and B [N][K] bf16
+ * row-major device matrices (16-byte aligned; M % 128 == 0, N % 64 == 0, K % 64 == 0), then
+ *   epi SBZ_MLP_F32:  out (float, row stride ldo) = D, or += D when accumulate;
+ *   epi SBZ_MLP_ACT:  z = D + bias; out (bf16) = act(z); z_out (bf16, may be NULL) = z;
+ *   epi SBZ_MLP_DACT: out (bf16) = D · act'(z_in);
+ * act SBZ_MLP_NONE or SBZ_MLP_SILU; only columns < n_valid (0: N) are written.  Queued on
+ * `stream`; the call waits for it and reports a pipeline timeout as SBZ_ERR_CUDA. */
+#define SBZ_MLP_F32 0
+#define SBZ_MLP_ACT 1
+#define SBZ_MLP_DACT 2
+#define SBZ_MLP_NONE 0
+#define SBZ_MLP_SILU 1
+int sbz_mlp_gemm(int M, int N, int K, const void* A, const void* B, int epi, int act, const float* bias, void* out, int ldo,
+                 int n_valid, int accumulate, void* z_out, const void* z_in, void* stream);
+
 /* spectrum_cmb(ΘlAs, ΘlBs, P0s, ls, ks) (src/observables/angular.jl:198-223): natural cubic
  * spline through (0,0) and (k, 2/π k² P0 Θ_A Θ_B), integrated exactly.  Th[ik*nl + il]. */
 int sbz_cl_integrate(int nk, const double* ks, const double* P0, int nl, const double* ThA,

@@ -1,0 +1,235 @@
+// BF16 tensor-core GEMM for the source surrogate's dense layers (sm_103a: TMA + tcgen05 + TMEM).
+//
+//   D[M x N] = A[M x K] · B[N x K]ᵀ   (A, B bf16 row-major with K contiguous, FP32 accumulation)
+//
+// One CTA computes a 128 x BN tile.  Warp 0 lane 0 streams 128 x 64 and BN x 64 K-slices into a
+// four-stage shared-memory ring with TMA (128-byte swizzle); warp 1 lane 0 issues
+// tcgen05.mma (kind::f16, M = 128, N = BN, K = 16) into a TMEM accumulator and releases ring
+// slots with tcgen05.commit; all four warps then read the accumulator with tcgen05.ld (warp w owns
+// TMEM lanes 32w..32w+31 = tile rows) and apply the fused epilogue:
+//   EPI_F32   out_f32 = D (+ out_f32 when accumulate)                      weight gradients
+//   EPI_ACT   z = D + bias; out = bf16(act(z)); optional z_out = bf16(z)    forward layers
+//   EPI_DACT  out = bf16(D · act'(z_in))                                   backward layers
+// Every mbarrier wait is bounded: a wait that runs out sets *err and the CTA skips ahead to its
+// TMEM release, so a fault in the pipeline cannot hang the GPU.
+#pragma once
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace sbz {
+namespace mlp {
+
+constexpr int BM = 128, BK = 64, STAGES = 4;
+constexpr unsigned kWaitLimit = 1u << 24;
+enum { EPI_F32 = 0, EPI_ACT = 1, EPI_DACT = 2 };
+enum { ACT_NONE = 0, ACT_SILU = 1 };
+
+struct GemmArgs {
+  int M, N, K;
+  int epi, act;
+  const float* bias;            // [N] (EPI_ACT), may be null
+  __nv_bfloat16* out_bf16;      // EPI_ACT / EPI_DACT
+  float* out_f32;               // EPI_F32
+  int ldo;                      // output row stride (elements)
+  int n_valid;                  // columns < n_valid are stored
+  int accumulate;               // EPI_F32: add to the output
+  __nv_bfloat16* z_out;         // EPI_ACT: pre-activation (ldo stride), may be null
+  const __nv_bfloat16* z_in;    // EPI_DACT: pre-activation of this layer (ldo stride)
+  unsigned* err;                // set to 1 by a CTA whose pipeline wait ran out
+};
+
+template <int BN>
+constexpr size_t gemm_smem_bytes() {
+  return 1024 /* alignment slack */ + (size_t)STAGES * (BM + BN) * BK * 2 + (2 * STAGES + 1) * 8 + 16;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
+  const uint32_t a = smem_u32(b);
+  for (unsigned i = 0; i < kWaitLimit; ++i) {
+    uint32_t ready;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ready)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ready) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// shared-memory matrix descriptor: K-major tile written by TMA with 128-byte swizzle
+// (rows of 128 B, 8-row groups 1024 B apart), start address in 16-byte units
+__device__ __forceinline__ uint64_t desc_sw128(const void* p) {
+  uint64_t d = (uint64_t)((smem_u32(p) & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;            // leading-dimension offset (unused by swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;  // stride-dimension offset: next 8-row group
+  d |= (uint64_t)1 << 46;            // descriptor version
+  d |= (uint64_t)2 << 61;            // 128-byte swizzle
+  return d;
+}
+
+template <int BN>
+__device__ __forceinline__ uint32_t idesc_bf16() {
+  return (1u << 4)                    // D: FP32
+         | (1u << 7) | (1u << 10)     // A, B: BF16
+         | ((uint32_t)(BN >> 3) << 17) // N
+         | ((uint32_t)(BM >> 4) << 24); // M
+}
+
+__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float dsilu(float z) {
+  const float s = 1.0f / (1.0f + __expf(-z));
+  return s * (1.0f + z * (1.0f - s));
+}
+
+template <int BN>
+__global__ void __launch_bounds__(128, 1) gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                         const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* sA = base;
+  unsigned char* sB = sA + (size_t)STAGES * BM * BK * 2;
+  uint64_t* full = (uint64_t*)(sB + (size_t)STAGES * BN * BK * 2);
+  uint64_t* empty = full + STAGES;
+  uint64_t* done = empty + STAGES;
+  uint32_t* tmem_slot = (uint32_t*)(done + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;
+  const int KT = g.K / BK;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)), "r"(BN) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  bool ok = true;
+  if (warp == 0 && lane == 0) {  // TMA producer
+    for (int kt = 0; kt < KT; ++kt) {
+      const int s = kt % STAGES;
+      const uint32_t ph = (uint32_t)(kt / STAGES) & 1u;
+      if (!mbar_wait(&empty[s], ph ^ 1u)) { ok = false; break; }
+      mbar_expect_tx(&full[s], (unsigned)((BM + BN) * BK * 2));
+      tma_load_2d(sA + (size_t)s * BM * BK * 2, &tmA, kt * BK, m0, &full[s]);
+      tma_load_2d(sB + (size_t)s * BN * BK * 2, &tmB, kt * BK, n0, &full[s]);
+    }
+  } else if (warp == 1 && lane == 0) {  // MMA issuer
+    const uint32_t idesc = idesc_bf16<BN>();
+    for (int kt = 0; kt < KT; ++kt) {
+      const int s = kt % STAGES;
+      const uint32_t ph = (uint32_t)(kt / STAGES) & 1u;
+      if (!mbar_wait(&full[s], ph)) { ok = false; break; }
+      tc_fence_after();
+      const uint64_t ad = desc_sw128(sA + (size_t)s * BM * BK * 2), bd = desc_sw128(sB + (size_t)s * BN * BK * 2);
+#pragma unroll
+      for (int kk = 0; kk < BK / 16; ++kk) {  // advance 16 elements = 32 B inside the swizzled row
+        const uint32_t acc = (kt | kk) != 0;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+            "l"(ad + 2 * kk), "l"(bd + 2 * kk), "r"(idesc), "r"(acc)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(&empty[s])) : "memory");
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(done)) : "memory");
+  }
+  __syncwarp();
+  // epilogue: thread = tile row m0 + 32 warp + lane
+  if (!mbar_wait(done, 0)) ok = false;
+  ok = __syncthreads_and(ok) != 0;  // CTA-uniform: the TMEM loads below are warp-collective
+  tc_fence_after();
+  const int row = m0 + warp * 32 + lane;
+  if (ok) {
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      uint32_t v[32];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%"
+          "22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]),
+            "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
+            "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]),
+            "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      const int col = n0 + c0;
+      if (row >= g.M || col >= g.n_valid) continue;
+      const size_t o = (size_t)row * g.ldo + col;
+      const int nv = min(32, g.n_valid - col);
+      if (g.epi == EPI_F32) {
+        float* out = g.out_f32 + o;
+        for (int j = 0; j < nv; ++j) {
+          const float d = __uint_as_float(v[j]);
+          out[j] = g.accumulate ? out[j] + d : d;
+        }
+      } else if (g.epi == EPI_ACT) {
+        __align__(16) __nv_bfloat16 y[32], zz[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const float z = __uint_as_float(v[j]) + (g.bias && j < nv ? g.bias[col + j] : 0.0f);
+          zz[j] = __float2bfloat16(z);
+          y[j] = __float2bfloat16(g.act == ACT_SILU ? silu(z) : z);
+        }
+        if (nv == 32 && (g.ldo % 8) == 0) {
+          uint4* dst = reinterpret_cast<uint4*>(g.out_bf16 + o);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) dst[q] = reinterpret_cast<const uint4*>(y)[q];
+          if (g.z_out) {
+            uint4* dz = reinterpret_cast<uint4*>(g.z_out + o);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) dz[q] = reinterpret_cast<const uint4*>(zz)[q];
+          }
+        } else {
+          for (int j = 0; j < nv; ++j) { g.out_bf16[o + j] = y[j]; if (g.z_out) g.z_out[o + j] = zz[j]; }
+        }
+      } else {  // EPI_DACT
+        __align__(16) __nv_bfloat16 y[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const float z = j < nv ? __bfloat162float(g.z_in[o + j]) : 0.0f;
+          y[j] = __float2bfloat16(__uint_as_float(v[j]) * (g.act == ACT_SILU ? dsilu(z) : 1.0f));
+        }
+        if (nv == 32 && (g.ldo % 8) == 0) {
+          uint4* dst = reinterpret_cast<uint4*>(g.out_bf16 + o);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) dst[q] = reinterpret_cast<const uint4*>(y)[q];
+        } else {
+          for (int j = 0; j < nv; ++j) g.out_bf16[o + j] = y[j];
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
+  if (!ok && lane == 0) atomicExch(g.err, 1u);
+}
+
+}  // namespace mlp
+}  // namespace sbz

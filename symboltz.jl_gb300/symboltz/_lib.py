@@ -20,7 +20,7 @@ EXPORTS = (
     "sbz_default_opts", "sbz_last_error", "sbz_momentum_quadrature", "sbz_problem_create", "sbz_problem_destroy",
     "sbz_problem_nstate", "sbz_solve_bg", "sbz_bg_knots", "sbz_bg_eval", "sbz_bg_coefficients", "sbz_solve_pt", "sbz_solve_pt_device", "sbz_pt_rhs",
     "sbz_spectrum_matter", "sbz_spectrum_primordial", "sbz_bessel_create", "sbz_bessel_destroy", "sbz_bessel_eval",
-    "sbz_los_integrate", "sbz_los_integrate_device", "sbz_cl_integrate", "sbz_cl_integrate_noalloc", "sbz_autotune_pt", "sbz_spectrum_cmb", "sbz_problem_set_stream",
+    "sbz_los_integrate", "sbz_los_integrate_device", "sbz_cl_integrate", "sbz_cl_integrate_noalloc", "sbz_autotune_pt", "sbz_mlp_gemm", "sbz_spectrum_cmb", "sbz_problem_set_stream",
     "sbz_problem_timings",
 )
 SBZ_KINTERP_SPLINE, SBZ_KINTERP_BARYCENTRIC = 0, 1
@@ -73,6 +73,7 @@ def lib():
     L.sbz_bg_coefficients.argtypes = [vp, C.c_int, C.c_int, dp, dp]
     L.sbz_solve_pt.argtypes = [vp, C.c_int, ip, dp, dp, C.c_int, dp, C.c_int, dp, ip, i64p]
     L.sbz_autotune_pt.argtypes = [vp, C.c_int, ip, dp, dp, C.c_int, dp, C.c_int, ip, dp]
+    L.sbz_mlp_gemm.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, C.c_int, C.c_int, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp]
     L.sbz_solve_pt_device.argtypes = [vp, C.c_int, vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp]
     L.sbz_pt_rhs.argtypes = [vp, C.c_int, ip, dp, dp, dp, dp, dp]
     L.sbz_spectrum_matter.argtypes = [vp, C.c_int, ip, dp, C.c_double, C.c_double, dp, ip]
