@@ -36,6 +36,8 @@ extern "C" {
 #define SBZ_OUT_SOURCES 0  /* k*S_T, k^2*S_E, S_psi at the saved times   (src/models/cosmologies.jl:99-105) */
 #define SBZ_OUT_DELTA_M 1  /* total matter Δ_m(τ0)                         (src/observables/fourier.jl:39-52) */
 #define SBZ_OUT_STATE 2    /* full perturbation state at the saved times   (solvept output_func = identity) */
+#define SBZ_OUT_SOURCES4 3 /* k*S_T split into k*(SW + ISW), k*Doppler, k*polarisation, and k^2*S_E
+                              (the four ST/SE terms of src/models/cosmologies.jl:99-104) */
 
 /* Cosmological parameters of one cosmology: parameters_Planck18 keys (src/parameters.jl:1-21). */
 typedef struct sbz_params {
@@ -101,7 +103,8 @@ int sbz_bg_coefficients(const sbz_problem* pb, int cosmo, int n, const double* t
 /* solvept (src/solve.jl:543-569) over nk modes: mode i belongs to cosmology cosmo[i] (NULL = all 0),
  * has wavenumber ks[i] and initial time tau_ini[i] (clamped to the background span, src/solve.jl:527).
  * Saved times: taus[c*ntau + j] for cosmology c (saveat).  out layout:
- *   SBZ_OUT_SOURCES: out[(i*ntau + j)*3 + s]; SBZ_OUT_DELTA_M: out[i]; SBZ_OUT_STATE: out[(i*ntau + j)*n + m].
+ *   SBZ_OUT_SOURCES: out[(i*ntau + j)*3 + s]; SBZ_OUT_DELTA_M: out[i]; SBZ_OUT_STATE: out[(i*ntau + j)*n + m];
+ *   SBZ_OUT_SOURCES4: out[(i*ntau + j)*4 + s].
  * status[i] per mode (may be NULL); steps[2i], steps[2i+1] = accepted, rejected (may be NULL). */
 int sbz_solve_pt(sbz_problem* pb, int nk, const int* cosmo, const double* ks, const double* tau_ini,
                  int ntau, const double* taus, int output, double* out, int* status, int64_t* steps);
@@ -151,6 +154,13 @@ int sbz_spectrum_cmb(sbz_problem* pb, int cosmo, const sbz_bessel* jl, int nc, c
                      const double* wc, int interp, int ntau, const double* taus, int nf, const double* ks_fine,
                      const double* yf, int npair, const int* pair_a, const int* pair_b, int l_limber, double* out_cl,
                      int* status);
+/* sbz_spectrum_cmb with the coarse sources supplied by the caller instead of the perturbation
+ * solve (no counterpart in the reference; used for surrogate sources): sources[(i*ntau + j)*3 + s]
+ * = (k S_T, k² S_E, S_ψ) at ks_coarse[i], taus[j], the SBZ_OUT_SOURCES layout. */
+int sbz_spectrum_cmb_sources(sbz_problem* pb, int cosmo, const sbz_bessel* jl, int nc, const double* ks_coarse, const double* yc,
+                             const double* wc, int interp, int ntau, const double* taus, const double* sources, int nf,
+                             const double* ks_fine, const double* yf, int npair, const int* pair_a, const int* pair_b, int l_limber,
+                             double* out_cl);
 /* Launch everything of this problem on an external CUDA stream (NULL: back to an own stream). */
 int sbz_problem_set_stream(sbz_problem* pb, void* stream);
 /* CUDA-event durations (ms) of the last sbz_spectrum_cmb: H2D, perturbations, k-interpolation,
@@ -182,6 +192,30 @@ int sbz_autotune_pt(sbz_problem* pb, int nk, const int* cosmo, const double* ks,
 #define SBZ_MLP_SILU 1
 int sbz_mlp_gemm(int M, int N, int K, const void* A, const void* B, int epi, int act, const float* bias, void* out, int ldo,
                  int n_valid, int accumulate, void* z_out, const void* z_in, void* stream);
+
+/* Source surrogate (sbz_surrogate_*; SURVEY-specified learned part, no counterpart in the reference):
+ * an MLP nin → nhidden × width (SiLU) → nout trained and evaluated with the BF16 tensor-core GEMM
+ * above (FP32 accumulation, FP32 master weights, Adam, MSE loss on the caller's normalised targets).
+ * nin, nout ≤ 64, width % 128 == 0, batch % 128 == 0.  Inputs/targets are host float arrays
+ * X[n][nin], Y[n][nout].  Parameters in flat order: per layer W[nout][nin] then b[nout]. */
+typedef struct sbz_surrogate sbz_surrogate;
+int sbz_surrogate_create(int nin, int width, int nhidden, int nout, int batch, unsigned long long seed, sbz_surrogate** out);
+void sbz_surrogate_destroy(sbz_surrogate* s);
+long long sbz_surrogate_nparams(const sbz_surrogate* s);
+int sbz_surrogate_get_params(const sbz_surrogate* s, float* params);
+int sbz_surrogate_set_params(sbz_surrogate* s, const float* params);
+/* Copy a training set to the device (replaces the previous one). */
+int sbz_surrogate_set_data(sbz_surrogate* s, long long n, const float* X, const float* Y);
+/* nsteps Adam steps (β = 0.9, 0.999) on batches drawn uniformly with replacement; *loss = mean
+ * squared error of the last batch. */
+int sbz_surrogate_train(sbz_surrogate* s, int nsteps, double lr, double* loss);
+/* Forward pass and gradients (flat parameter order) of the mean squared error on exactly these
+ * n rows (n % 128 == 0, n ≤ batch); the weights are not changed. */
+int sbz_surrogate_gradients(sbz_surrogate* s, int n, const float* X, const float* Y, double* loss, float* grads);
+int sbz_surrogate_infer(sbz_surrogate* s, long long n, const float* X, float* Y);
+/* Flat binary weight file: "SBZMLP01", int32 nin, width, nhidden, nout, FP32 parameters. */
+int sbz_surrogate_save(const sbz_surrogate* s, const char* path);
+int sbz_surrogate_load(const char* path, int batch, sbz_surrogate** out);
 
 /* spectrum_cmb(ΘlAs, ΘlBs, P0s, ls, ks) (src/observables/angular.jl:198-223): natural cubic
  * spline through (0,0) and (k, 2/π k² P0 Θ_A Θ_B), integrated exactly.  Th[ik*nl + il]. */

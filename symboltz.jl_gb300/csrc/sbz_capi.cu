@@ -346,7 +346,7 @@ static int pt_run(sbz_problem* pb, int nk, const int* d_cosmo, const double* d_k
 static bool check_pt_args(sbz_problem* pb, int nk, int ntau, int output) {
   if (!pb || !pb->bg_done) { fail(SBZ_ERR_STATE, "call sbz_solve_bg first"); return false; }
   if (upload_tables(pb) != SBZ_OK) return false;
-  if (nk < 0 || ntau < 0 || output < SBZ_OUT_SOURCES || output > SBZ_OUT_STATE) { fail(SBZ_ERR_ARG, "bad sizes or output"); return false; }
+  if (nk < 0 || ntau < 0 || output < SBZ_OUT_SOURCES || output > SBZ_OUT_SOURCES4) { fail(SBZ_ERR_ARG, "bad sizes or output"); return false; }
   if (output != SBZ_OUT_DELTA_M && ntau == 0) { fail(SBZ_ERR_ARG, "saved times required"); return false; }
   return true;
 }
@@ -401,7 +401,8 @@ int sbz_solve_pt(sbz_problem* pb, int nk, const int* cosmo, const double* ks, co
     if (c < 0 || c >= pb->ncosmo) return fail(SBZ_ERR_ARG, "cosmology index out of range");
   }
   const int n = pb->M.n;
-  const size_t nout = output == SBZ_OUT_DELTA_M ? (size_t)nk : output == SBZ_OUT_SOURCES ? (size_t)nk * ntau * 3 : (size_t)nk * ntau * n;
+  const size_t nout = output == SBZ_OUT_DELTA_M ? (size_t)nk : output == SBZ_OUT_SOURCES ? (size_t)nk * ntau * 3
+                      : output == SBZ_OUT_SOURCES4 ? (size_t)nk * ntau * 4 : (size_t)nk * ntau * n;
   // longest-first work order: high-k modes take the most steps
   std::vector<int> order(nk);
   std::iota(order.begin(), order.end(), 0);
@@ -452,7 +453,8 @@ int sbz_autotune_pt(sbz_problem* pb, int nk, const int* cosmo, const double* ks,
     sk.push_back(ks[j]); st.push_back(tau_ini[j]); sc.push_back(c); order.push_back((int)order.size());
   }
   const int ns = (int)sk.size(), n = pb->M.n;
-  const size_t nout = output == SBZ_OUT_DELTA_M ? (size_t)ns : output == SBZ_OUT_SOURCES ? (size_t)ns * ntau * 3 : (size_t)ns * ntau * n;
+  const size_t nout = output == SBZ_OUT_DELTA_M ? (size_t)ns : output == SBZ_OUT_SOURCES ? (size_t)ns * ntau * 3
+                      : output == SBZ_OUT_SOURCES4 ? (size_t)ns * ntau * 4 : (size_t)ns * ntau * n;
   cudaStream_t s = pb->stream;
   SBZ_CUDA(pb->d_k.ensure(sizeof(double) * ns));
   SBZ_CUDA(pb->d_ti.ensure(sizeof(double) * ns));
@@ -517,9 +519,31 @@ int sbz_spectrum_matter(sbz_problem* pb, int nk, const int* cosmo, const double*
   return SBZ_OK;
 }
 
+static int spectrum_cmb_impl(sbz_problem* pb, int cosmo, const sbz_bessel* jl, int nc, const double* ks_coarse, const double* yc,
+                             const double* wc, int interp, int ntau, const double* taus, const double* coarse_sources, int nf,
+                             const double* ks_fine, const double* yf, int npair, const int* pair_a, const int* pair_b, int l_limber,
+                             double* out_cl, int* status);
+
 int sbz_spectrum_cmb(sbz_problem* pb, int cosmo, const sbz_bessel* jl, int nc, const double* ks_coarse, const double* yc,
                      const double* wc, int interp, int ntau, const double* taus, int nf, const double* ks_fine, const double* yf,
                      int npair, const int* pair_a, const int* pair_b, int l_limber, double* out_cl, int* status) {
+  return spectrum_cmb_impl(pb, cosmo, jl, nc, ks_coarse, yc, wc, interp, ntau, taus, nullptr, nf, ks_fine, yf, npair, pair_a, pair_b,
+                           l_limber, out_cl, status);
+}
+
+int sbz_spectrum_cmb_sources(sbz_problem* pb, int cosmo, const sbz_bessel* jl, int nc, const double* ks_coarse, const double* yc,
+                             const double* wc, int interp, int ntau, const double* taus, const double* sources, int nf,
+                             const double* ks_fine, const double* yf, int npair, const int* pair_a, const int* pair_b, int l_limber,
+                             double* out_cl) {
+  if (!sources) return fail(SBZ_ERR_ARG, "null sources");
+  return spectrum_cmb_impl(pb, cosmo, jl, nc, ks_coarse, yc, wc, interp, ntau, taus, sources, nf, ks_fine, yf, npair, pair_a, pair_b,
+                           l_limber, out_cl, nullptr);
+}
+
+static int spectrum_cmb_impl(sbz_problem* pb, int cosmo, const sbz_bessel* jl, int nc, const double* ks_coarse, const double* yc,
+                             const double* wc, int interp, int ntau, const double* taus, const double* coarse_sources, int nf,
+                             const double* ks_fine, const double* yf, int npair, const int* pair_a, const int* pair_b, int l_limber,
+                             double* out_cl, int* status) {
   if (!pb || !jl || !ks_coarse || !yc || !taus || !ks_fine || !yf || !pair_a || !pair_b || !out_cl) return fail(SBZ_ERR_ARG, "null argument");
   if (nc < 3 || ntau < 2 || nf < 2 || npair < 1 || cosmo < 0 || cosmo >= pb->ncosmo) return fail(SBZ_ERR_ARG, "bad sizes");
   if (interp == SBZ_KINTERP_BARYCENTRIC && !wc) return fail(SBZ_ERR_ARG, "barycentric weights required");
@@ -610,8 +634,11 @@ int sbz_spectrum_cmb(sbz_problem* pb, int cosmo, const sbz_bessel* jl, int nc, c
   SBZ_CUDA(pb->d_status.ensure(sizeof(int) * nc));
   SBZ_CUDA(pb->d_steps.ensure(sizeof(int64_t) * 2 * nc));
   SBZ_CUDA(cudaEventRecord(pb->ev[1], st));
-  // 1. perturbation modes -> coarse sources
-  {
+  // 1. perturbation modes -> coarse sources (or the caller's coarse sources, e.g. a surrogate's)
+  if (coarse_sources) {
+    SBZ_CUDA(cudaMemcpyAsync(pb->d_out.p, coarse_sources, sizeof(double) * (size_t)nc * ntau * 3, cudaMemcpyHostToDevice, st));
+    SBZ_CUDA(cudaMemsetAsync(pb->d_status.p, 0, sizeof(int) * nc, st));
+  } else {
     sbz::PtArgs A{};
     A.model = pb->d_model.as<sbz::ModelDesc>(); A.comps = pb->d_comps.as<sbz::CompDesc>(); A.model_n = pb->M.n;
     A.cosmos = pb->d_cosmos.as<sbz::CosmoDesc>(); A.tables = pb->d_tables.as<double>(); A.table_stride = pb->table_stride;

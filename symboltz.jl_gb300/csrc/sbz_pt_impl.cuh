@@ -732,7 +732,7 @@ __device__ void emit_output(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const PtA
     for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) o[i] = y[sl]; }
     return;
   }
-  if (A.output != SBZ_OUT_SOURCES) return;
+  if (A.output != SBZ_OUT_SOURCES && A.output != SBZ_OUT_SOURCES4) return;
   // line-of-sight sources (src/models/cosmologies.jl:99-105)
   const int so = kNSets - 1;
   const double k = mk.k;
@@ -760,13 +760,19 @@ __device__ void emit_output(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const PtA
       const double Pi = W.x[7] + W.x[8] + W.x[10];
       const double Pid = W.f[7] + W.f[8] + W.f[10];
       const double psid = dpsi_w + psi_f;  // Ψ' = (∂Ψ/∂τ) y + Ψ(f)
-      const double sT = v * (W.x[5] * 0.25 + psi + Pi / 16) + ek * (psid + phid) + (vd * W.x[4] + v * W.f[4]) * mk.ik2 +
-                        3.0 / 16.0 * mk.ik2 * (vdd * Pi + 2 * vd * Pid + v * Pidd);
+      const double sSW = v * (W.x[5] * 0.25 + psi + Pi / 16), sISW = ek * (psid + phid);
+      const double sDop = (vd * W.x[4] + v * W.f[4]) * mk.ik2;
+      const double sPol = 3.0 / 16.0 * mk.ik2 * (vdd * Pi + 2 * vd * Pid + v * Pidd);
       const double chi = cd->tau0 - tau;
       const double SE = 3.0 / 16.0 * v * Pi / ((k * chi) * (k * chi));
-      const double Spsi = (tau >= cd->taurec) ? -(psi + W.x[0]) * (tau - cd->taurec) / (cd->tau0 - cd->taurec) / chi : 0.0;
-      double* o = A.out + ((size_t)item * A.ntau + j) * 3;
-      o[0] = k * sT; o[1] = k * k * SE; o[2] = Spsi;
+      if (A.output == SBZ_OUT_SOURCES4) {
+        double* o = A.out + ((size_t)item * A.ntau + j) * 4;
+        o[0] = k * (sSW + sISW); o[1] = k * sDop; o[2] = k * sPol; o[3] = k * k * SE;
+      } else {
+        const double Spsi = (tau >= cd->taurec) ? -(psi + W.x[0]) * (tau - cd->taurec) / (cd->tau0 - cd->taurec) / chi : 0.0;
+        double* o = A.out + ((size_t)item * A.ntau + j) * 3;
+        o[0] = k * (sSW + sISW + sDop + sPol); o[1] = k * k * SE; o[2] = Spsi;
+      }
     }
   }
   g.sync();
@@ -883,6 +889,8 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
       while (jout < A.ntau && taus[jout] <= t) {
         if (taus[jout] < t) {  // before the mode starts: zero
           if (A.output == SBZ_OUT_SOURCES && gt < 3) A.out[((size_t)item * A.ntau + jout) * 3 + gt] = 0;
+        if (A.output == SBZ_OUT_SOURCES4 && gt < 4) A.out[((size_t)item * A.ntau + jout) * 4 + gt] = 0;
+          if (A.output == SBZ_OUT_SOURCES4 && gt < 4) A.out[((size_t)item * A.ntau + jout) * 4 + gt] = 0;
           if (A.output == SBZ_OUT_STATE) for (int i = gt; i < n; i += NT) A.out[((size_t)item * A.ntau + jout) * n + i] = 0;
         } else {
           emit_output(g, W, A, cd, tab, comps, M, mk, t, y, item, jout);
@@ -1095,6 +1103,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
     if (taus) {
       for (; jout < A.ntau; ++jout) {
         if (A.output == SBZ_OUT_SOURCES && gt < 3) A.out[((size_t)item * A.ntau + jout) * 3 + gt] = 0;
+        if (A.output == SBZ_OUT_SOURCES4 && gt < 4) A.out[((size_t)item * A.ntau + jout) * 4 + gt] = 0;
         if (A.output == SBZ_OUT_STATE) for (int i = gt; i < n; i += NT) A.out[((size_t)item * A.ntau + jout) * n + i] = 0;
       }
     }

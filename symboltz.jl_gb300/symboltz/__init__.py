@@ -175,7 +175,7 @@ def solvebg(prob: CosmologyProblem):
     return prob.solvebg()
 
 
-_OUT = {"sources": L.SBZ_OUT_SOURCES, "delta_m": L.SBZ_OUT_DELTA_M, "state": L.SBZ_OUT_STATE}
+_OUT = {"sources": L.SBZ_OUT_SOURCES, "delta_m": L.SBZ_OUT_DELTA_M, "state": L.SBZ_OUT_STATE, "sources4": L.SBZ_OUT_SOURCES4}
 
 
 def autotune(prob: CosmologyProblem, ks, ptivini=-np.inf, *, saveat=None, output="sources", cosmo=None):
@@ -226,7 +226,8 @@ def solvept(prob: CosmologyProblem, ks, ptivini=-np.inf, *, saveat=None, output=
         taus = np.broadcast_to(taus, (prob.ncosmo, taus.shape[-1])) if taus.ndim == 1 else taus
     taus = L.f64(taus)
     ntau = taus.shape[1]
-    shape = {L.SBZ_OUT_DELTA_M: (nk,), L.SBZ_OUT_SOURCES: (nk, ntau, 3), L.SBZ_OUT_STATE: (nk, ntau, prob.nstate)}[kind]
+    shape = {L.SBZ_OUT_DELTA_M: (nk,), L.SBZ_OUT_SOURCES: (nk, ntau, 3), L.SBZ_OUT_SOURCES4: (nk, ntau, 4),
+             L.SBZ_OUT_STATE: (nk, ntau, prob.nstate)}[kind]
     out = np.zeros(shape)
     st = np.zeros(nk, dtype=np.int32)
     steps = np.zeros((nk, 2), dtype=np.int64)
@@ -471,7 +472,8 @@ def spectrum_cmb(*args, **kw):
 
 
 def _spectrum_cmb_driver(modes, prob: CosmologyProblem, jl: SphericalBesselCache, ls_out=None, *, normalization="Cl",
-                         kinterp=None, Δkτ0=np.pi, xs=None, τcut=1e-2, l_limber=10, cosmo=0, taus=None, return_status=False):
+                         kinterp=None, Δkτ0=np.pi, xs=None, τcut=1e-2, l_limber=10, cosmo=0, taus=None, return_status=False,
+                         sources=None):
     """Grids as in the reference driver; everything after them runs in one device pipeline
     (sbz_spectrum_cmb): coarse solve -> k-interpolation -> line of sight -> Θ scaling -> C_l."""
     modes = [modes] if isinstance(modes, str) else list(modes)
@@ -505,9 +507,16 @@ def _spectrum_cmb_driver(modes, prob: CosmologyProblem, jl: SphericalBesselCache
     nl = len(ls)
     Cl = np.zeros((len(modes), nl))
     st = np.zeros(len(xs_c), dtype=np.int32)
-    L.check(L.lib().sbz_spectrum_cmb(prob._h, cosmo, jl._h, len(xs_c), L.dptr(xs_c), L.dptr(yc), L.dptr(wc), kind,
-                                     len(taus), L.dptr(taus), len(ks_fine), L.dptr(L.f64(ks_fine)), L.dptr(yf), len(modes),
-                                     L.iptr(pa), L.iptr(pb), int(l_limber), L.dptr(Cl), L.iptr(st)), "spectrum_cmb")
+    if sources is None:
+        L.check(L.lib().sbz_spectrum_cmb(prob._h, cosmo, jl._h, len(xs_c), L.dptr(xs_c), L.dptr(yc), L.dptr(wc), kind,
+                                         len(taus), L.dptr(taus), len(ks_fine), L.dptr(L.f64(ks_fine)), L.dptr(yf), len(modes),
+                                         L.iptr(pa), L.iptr(pb), int(l_limber), L.dptr(Cl), L.iptr(st)), "spectrum_cmb")
+    else:  # coarse sources supplied by the caller (k S_T, k² S_E, S_ψ) on (kinterp.xs, taus)
+        src = L.f64(np.asarray(sources, dtype=np.float64).reshape(len(xs_c), len(taus), 3))
+        L.check(L.lib().sbz_spectrum_cmb_sources(prob._h, cosmo, jl._h, len(xs_c), L.dptr(xs_c), L.dptr(yc), L.dptr(wc), kind,
+                                                 len(taus), L.dptr(taus), L.dptr(src), len(ks_fine), L.dptr(L.f64(ks_fine)),
+                                                 L.dptr(yf), len(modes), L.iptr(pa), L.iptr(pb), int(l_limber), L.dptr(Cl)),
+                "spectrum_cmb_sources")
     out = Cl.T.copy()
     if normalization == "Dl":
         out *= (ls * (ls + 1) / (2 * np.pi))[:, None]

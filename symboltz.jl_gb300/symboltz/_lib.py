@@ -14,13 +14,15 @@ LIB_PATH = os.path.join(PKG, "lib", "libsymboltz_gb300.so")
 SBZ_OK, SBZ_MAXITERS, SBZ_DTMIN, SBZ_NONFINITE = 0, 1, 2, 3
 SBZ_ERR_ARG, SBZ_ERR_CUDA, SBZ_ERR_NOMEM, SBZ_ERR_STATE = -1, -2, -3, -4
 SBZ_FP64, SBZ_MIXED = 0, 1
-SBZ_OUT_SOURCES, SBZ_OUT_DELTA_M, SBZ_OUT_STATE = 0, 1, 2
+SBZ_OUT_SOURCES, SBZ_OUT_DELTA_M, SBZ_OUT_STATE, SBZ_OUT_SOURCES4 = 0, 1, 2, 3
 
 EXPORTS = (
     "sbz_default_opts", "sbz_last_error", "sbz_momentum_quadrature", "sbz_problem_create", "sbz_problem_destroy",
     "sbz_problem_nstate", "sbz_solve_bg", "sbz_bg_knots", "sbz_bg_eval", "sbz_bg_coefficients", "sbz_solve_pt", "sbz_solve_pt_device", "sbz_pt_rhs",
     "sbz_spectrum_matter", "sbz_spectrum_primordial", "sbz_bessel_create", "sbz_bessel_destroy", "sbz_bessel_eval",
-    "sbz_los_integrate", "sbz_los_integrate_device", "sbz_cl_integrate", "sbz_cl_integrate_noalloc", "sbz_autotune_pt", "sbz_mlp_gemm", "sbz_spectrum_cmb", "sbz_problem_set_stream",
+    "sbz_los_integrate", "sbz_los_integrate_device", "sbz_cl_integrate", "sbz_cl_integrate_noalloc", "sbz_autotune_pt", "sbz_mlp_gemm", "sbz_surrogate_create", "sbz_surrogate_destroy", "sbz_surrogate_nparams",
+    "sbz_surrogate_get_params", "sbz_surrogate_set_params", "sbz_surrogate_set_data", "sbz_surrogate_train",
+    "sbz_surrogate_gradients", "sbz_surrogate_infer", "sbz_surrogate_save", "sbz_surrogate_load", "sbz_spectrum_cmb", "sbz_spectrum_cmb_sources", "sbz_problem_set_stream",
     "sbz_problem_timings",
 )
 SBZ_KINTERP_SPLINE, SBZ_KINTERP_BARYCENTRIC = 0, 1
@@ -73,6 +75,20 @@ def lib():
     L.sbz_bg_coefficients.argtypes = [vp, C.c_int, C.c_int, dp, dp]
     L.sbz_solve_pt.argtypes = [vp, C.c_int, ip, dp, dp, C.c_int, dp, C.c_int, dp, ip, i64p]
     L.sbz_autotune_pt.argtypes = [vp, C.c_int, ip, dp, dp, C.c_int, dp, C.c_int, ip, dp]
+    fp = C.POINTER(C.c_float)
+    L.sbz_surrogate_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(vp)]
+    L.sbz_surrogate_destroy.argtypes = [vp]
+    L.sbz_surrogate_destroy.restype = None
+    L.sbz_surrogate_nparams.argtypes = [vp]
+    L.sbz_surrogate_nparams.restype = C.c_longlong
+    L.sbz_surrogate_get_params.argtypes = [vp, fp]
+    L.sbz_surrogate_set_params.argtypes = [vp, fp]
+    L.sbz_surrogate_set_data.argtypes = [vp, C.c_longlong, fp, fp]
+    L.sbz_surrogate_train.argtypes = [vp, C.c_int, C.c_double, dp]
+    L.sbz_surrogate_gradients.argtypes = [vp, C.c_int, fp, fp, dp, fp]
+    L.sbz_surrogate_infer.argtypes = [vp, C.c_longlong, fp, fp]
+    L.sbz_surrogate_save.argtypes = [vp, C.c_char_p]
+    L.sbz_surrogate_load.argtypes = [C.c_char_p, C.c_int, C.POINTER(vp)]
     L.sbz_mlp_gemm.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, C.c_int, C.c_int, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp]
     L.sbz_solve_pt_device.argtypes = [vp, C.c_int, vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp]
     L.sbz_pt_rhs.argtypes = [vp, C.c_int, ip, dp, dp, dp, dp, dp]
@@ -89,6 +105,8 @@ def lib():
                                            C.c_void_p]
     L.sbz_spectrum_cmb.argtypes = [vp, C.c_int, vp, C.c_int, dp, dp, dp, C.c_int, C.c_int, dp, C.c_int, dp, dp, C.c_int,
                                    ip, ip, C.c_int, dp, ip]
+    L.sbz_spectrum_cmb_sources.argtypes = [vp, C.c_int, vp, C.c_int, dp, dp, dp, C.c_int, C.c_int, dp, dp, C.c_int, dp, dp, C.c_int,
+                                           ip, ip, C.c_int, dp]
     L.sbz_problem_set_stream.argtypes = [vp, vp]
     L.sbz_problem_timings.argtypes = [vp, dp]
     _lib = L

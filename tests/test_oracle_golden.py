@@ -147,3 +147,19 @@ def test_pk_self_convergence():
 def test_failed_modes_report_status(bg5):
     _, st, _ = bg5.solve_pt(np.array([0.0, np.nan, 1.0]), 1e-4, mode=1)
     assert st[0] != 0 and st[1] != 0 and st[2] == 0
+
+
+def test_mlp_oracle_gradient_matches_finite_differences():
+    """The MLP oracle's backpropagation against central finite differences (FP64)."""
+    import mlp as MO
+    rng = np.random.default_rng(3)
+    sizes = MO.layer_sizes(3, 8, 2, 2)
+    n = sum(a * b + b for a, b in zip(sizes[:-1], sizes[1:]))
+    p = rng.normal(0, 0.5, n)
+    X, Y = rng.normal(size=(5, 3)), rng.normal(size=(5, 2))
+    loss, g = MO.loss_and_grad(p, X, Y, sizes)
+    h = 1e-6
+    fd = np.array([(MO.loss_and_grad(p + h * e, X, Y, sizes)[0] - MO.loss_and_grad(p - h * e, X, Y, sizes)[0]) / (2 * h)
+                   for e in np.eye(n)])
+    np.testing.assert_allclose(g, fd, rtol=1e-6, atol=1e-9)
+    assert MO.bf16_round(np.array([1.0, 1.00390625, 3.14159]))[2] == 3.140625
