@@ -142,7 +142,7 @@ class SourceSurrogate:
 
     def solve_sources(self, thetas, precision="mixed", ks=None):
         """Solver sources4 for each θ on (ks or the coarse grid) × its own τ grid:
-        returns (sources [ncos][nk][ntau][4], taus [ncos][ntau], problem)."""
+        returns (sources [ncos][nk][ntau][4], taus [ncos][ntau], envelopes [ncos][ntau], problem)."""
         from . import CosmologyProblem, solvept
         ks = self.ks if ks is None else np.asarray(ks, dtype=np.float64)
         prob = CosmologyProblem(self.M, [box_params(t) for t in thetas], precision=precision)
@@ -155,13 +155,43 @@ class SourceSurrogate:
         out, st, _ = solvept(prob, np.tile(ks, len(thetas)), prob.opts.tau_ini, saveat=taus, output="sources4", cosmo=cos)
         if np.any(st != 0):
             raise L.SbzError(f"{int(np.count_nonzero(st))} training modes failed")
-        return out.reshape(len(thetas), nk, self.ntau, 4), taus, prob
+        out = out.reshape(len(thetas), nk, self.ntau, 4)
+        out[:, :, -1, :] = 0.0  # χ = 0: zeroed, as the line of sight does (src/observables/angular.jl:296)
+        env = np.stack([self.envelope(bg.eval(taus[c], c)) for c in range(len(thetas))])
+        return out, taus, env, prob
+
+    @staticmethod
+    def envelope(bgv):
+        """|v| + e^{-κ} + 1e-3 max|v| from background columns (…, κ, v, …): the visibility and
+        transparency factors the sources carry, so that sources / envelope are smooth in τ."""
+        v, kappa = bgv[:, 4], bgv[:, 3]
+        return np.abs(v) + np.exp(-kappa) + 1e-3 * np.max(np.abs(v))
+
+    @staticmethod
+    def _chi2(taus):
+        return (taus[-1] - taus) ** 2  # χ² = (τ0 - τ)²
+
+    def to_targets(self, S4, taus, env):
+        """Learned quantities for sources4 [nk][ntau][4] on one cosmology's τ grid: the three
+        temperature terms and χ² k² S_E = (3/16) v Π (removing the 1/χ² of S_E), each divided by the
+        cosmology's visibility envelope (the sharp recombination peak is known exactly from the
+        background; the network learns the smooth factors multiplying it)."""
+        Y = S4.copy()
+        Y[..., 3] *= self._chi2(taus)
+        return Y / env[None, :, None]
+
+    def from_targets(self, Y, taus, env):
+        S4 = Y * env[None, :, None]
+        chi2 = self._chi2(taus)
+        S4[..., 3] = np.where(chi2 > 0, S4[..., 3] / np.where(chi2 > 0, chi2, 1.0), 0.0)
+        S4[:, -1, :] = 0.0
+        return S4
 
     def dataset(self, thetas):
         """(X, Y, taus) training arrays from the solver for the given parameter points."""
-        S, taus, _ = self.solve_sources(thetas)
+        S, taus, env, _ = self.solve_sources(thetas)
         X = np.concatenate([self.features(t, taus[c]) for c, t in enumerate(thetas)])
-        Y = S.reshape(-1, 4)
+        Y = np.concatenate([self.to_targets(S[c], taus[c], env[c]).reshape(-1, 4) for c in range(len(thetas))])
         return X, Y, taus
 
     # ---- training ---------------------------------------------------------------------------
@@ -181,9 +211,14 @@ class SourceSurrogate:
             done += n
         return losses
 
+    def mse(self, X, Y):
+        """Mean squared error of the network on (X, Y) in standardised units (all rows)."""
+        P = self.net.infer(X).astype(np.float64)
+        return float(np.mean((P - (Y - self.mean) / self.scale) ** 2))
+
     # ---- prediction ------------------------------------------------------------------------
-    def predict(self, theta, taus, ks=None):
-        """Sources4 [nk][ntau][4] for one cosmology (physical units)."""
+    def predict(self, theta, taus, env, ks=None):
+        """Sources4 [nk][ntau][4] for one cosmology (physical units); env: its visibility envelope."""
         if ks is not None:
             keep, self.ks = self.ks, np.asarray(ks, dtype=np.float64)
             try:
@@ -192,8 +227,8 @@ class SourceSurrogate:
                 self.ks = keep
         else:
             X = self.features(theta, taus)
-        Y = self.net.infer(X).astype(np.float64) * self.scale + self.mean
-        return Y.reshape(-1, len(taus), 4)
+        Y = (self.net.infer(X).astype(np.float64) * self.scale + self.mean).reshape(-1, len(taus), 4)
+        return self.from_targets(Y, taus, env)
 
     @staticmethod
     def los_sources(S4):
@@ -207,9 +242,9 @@ class SourceSurrogate:
         self.net.save(path)
         np.savez(str(path) + ".norm.npz", mean=self.mean, scale=self.scale, ks=self.ks, ntau=self.ntau)
 
-    def probe_error(self, theta, taus, S4_true, kprobe):
+    def probe_error(self, theta, taus, env, S4_true, kprobe):
         """Relative L2 error of the predicted sources against solver sources at the probe modes."""
-        P = self.predict(theta, taus, ks=kprobe)
+        P = self.predict(theta, taus, env, ks=kprobe)
         return float(np.linalg.norm(P - S4_true) / (np.linalg.norm(S4_true) + 1e-300))
 
     def spectra(self, thetas, jl, ls_out, kinterp, modes=("TT", "TE", "EE"), tol=0.05, kprobe=None, fallback=True):
@@ -218,8 +253,8 @@ class SourceSurrogate:
         probe errors, fallback mask)."""
         from . import CosmologyProblem, spectrum_cmb
         kprobe = np.geomspace(self.ks.min() * 10, self.ks.max() / 3, 4) if kprobe is None else np.asarray(kprobe)
-        S4p, taus, prob = self.solve_sources(thetas, ks=kprobe)
-        errs = np.array([self.probe_error(t, taus[c], S4p[c], kprobe) for c, t in enumerate(thetas)])
+        S4p, taus, env, prob = self.solve_sources(thetas, ks=kprobe)
+        errs = np.array([self.probe_error(t, taus[c], env[c], S4p[c], kprobe) for c, t in enumerate(thetas)])
         fb = (errs > tol) if fallback else np.zeros(len(thetas), dtype=bool)
         out = []
         for c, t in enumerate(thetas):
@@ -227,7 +262,7 @@ class SourceSurrogate:
                 p1 = CosmologyProblem(self.M, box_params(t))
                 out.append(spectrum_cmb(list(modes), p1, jl, ls_out, kinterp=kinterp, taus=taus[c], normalization="Dl"))
             else:
-                src = self.los_sources(self.predict(t, taus[c], ks=kinterp.xs))
+                src = self.los_sources(self.predict(t, taus[c], env[c], ks=kinterp.xs))
                 out.append(spectrum_cmb(list(modes), prob, jl, ls_out, kinterp=kinterp, taus=taus[c], cosmo=c, normalization="Dl",
                                         sources=src))
         return np.stack(out), errs, fb

@@ -82,8 +82,10 @@ def test_surrogate_sources_through_the_line_of_sight_with_fallback():
     train = sample_box(4, seed=0)
     X, Y, _ = sur.dataset(train)
     assert X.shape == (4 * 32 * 48, 8) and np.all(np.isfinite(Y))
-    losses = sur.fit(X, Y, steps=300, lr=2e-3, lr_final=2e-4, chunks=3)
-    assert losses[-1] < losses[0]
+    sur.fit(X, Y, steps=1, lr=1e-4)
+    before = sur.mse(X, Y)
+    sur.fit(X, Y, steps=400, lr=2e-3, lr_final=2e-4, chunks=4)
+    assert sur.mse(X, Y) < before  # learning quality is measured at full resolution (bench); here the plumbing
     test = sample_box(2, seed=1)
     jl = S.SphericalBesselCache(np.arange(2, 401, 10))
     kin = S.CubicSplineInterpolator(ks, f=np.log)
@@ -93,7 +95,7 @@ def test_surrogate_sources_through_the_line_of_sight_with_fallback():
     Dfb, err2, fb2 = sur.spectra(test, jl, ls, kin, tol=0.0)
     assert fb2.all()
     np.testing.assert_allclose(err2, err)
-    _, taus, _ = sur.solve_sources(test[:1])
+    _, taus, _, _ = sur.solve_sources(test[:1])
     ref = S.spectrum_cmb(["TT", "TE", "EE"], S.CosmologyProblem(M, box_params(test[0])), jl, ls, kinterp=kin, taus=taus[0],
                          normalization="Dl")
     np.testing.assert_allclose(Dfb[0], ref, rtol=1e-12)
