@@ -346,6 +346,74 @@ def run_batched(args):
     print(json.dumps(line), flush=True)
 
 
+def run_surrogate(args):
+    """Learned part: training data from the GPU solver (scrambled-Sobol box points; perturbation
+    factors on 400 k × 500 τ), training with the library's BF16 tcgen05 kernels, then C_l (D_l, TT/TE/EE
+    to l = 2500) of held-out cosmologies through surrogate + solver fallback, judged against the
+    all-FP64 solver; cosmologies/s of that path against the plain (mixed-precision) solver path."""
+    import torch
+    import symboltz as S
+    from symboltz import surrogate as SG
+    assert torch.cuda.is_available(), "bench needs a GPU"
+    M = S.ΛCDM(lmax_gamma=MODEL["lmax_gamma"], lmax_nu=MODEL["lmax_nu"], lmax_h=MODEL["lmax_h"], nx=MODEL["nx"])
+    ks = S.k_from_hMpc(S.loggrid(1e-4, 0.5, length=400))
+    sur = SG.SourceSurrogate(M, ks, ntau=500, width=512, nhidden=4, batch=65536, seed=0)
+    t0 = time.perf_counter()
+    X, Y, _ = sur.dataset(SG.sample_box(args.train_cosmologies, seed=0, sobol=True))
+    t_data = time.perf_counter() - t0
+    losses, steps, t_train = [], 0, 0.0
+    sur.fit(X, Y, steps=1, lr=1e-3)
+    while t_train < args.train_seconds:
+        t1 = time.perf_counter()
+        frac = t_train / args.train_seconds
+        losses.append(sur.net.train(200, 1e-3 * (1e-2) ** frac))
+        t_train += time.perf_counter() - t1
+        steps += 200
+    mse_train = sur.mse(X[:: max(1, len(X) // 2_000_000)], Y[:: max(1, len(X) // 2_000_000)])
+    del X, Y
+    flops_step = 3 * 2 * 65536 * (64 * 512 + 3 * 512 * 512 + 512 * 64)  # forward + 2 backward GEMM sets
+    test = SG.sample_box(args.test_cosmologies, seed=1)
+    ls = np.unique(np.round(np.exp(np.linspace(np.log(2), np.log(LMAX), 200))).astype(np.int32))
+    jl = S.SphericalBesselCache(ls)
+    kin = S.CubicSplineInterpolator(ks, f=np.log)
+    lall = np.arange(2, LMAX + 1)
+    # judge: all-FP64 solver on the same grids
+    _, taus, _, _ = sur.solve_factors(test[:1])
+    judge, t_solver = [], 0.0
+    for th in test:
+        p64 = S.CosmologyProblem(M, SG.box_params(th), precision="fp64")
+        bg = p64.solvebg()
+        tt = SG.cmb_taus(bg.t(0), bg.tau0[0], sur.ntau)
+        judge.append(S.spectrum_cmb(["TT", "TE", "EE"], p64, jl, lall, kinterp=kin, taus=tt, normalization="Dl"))
+        pm = S.CosmologyProblem(M, SG.box_params(th))
+        t1 = time.perf_counter()
+        bgm = pm.solvebg()
+        S.spectrum_cmb(["TT", "TE", "EE"], pm, jl, lall, kinterp=kin, taus=SG.cmb_taus(bgm.t(0), bgm.tau0[0], sur.ntau), normalization="Dl")
+        t_solver += time.perf_counter() - t1
+    judge = np.stack(judge)
+    t1 = time.perf_counter()
+    Dl, errs, fb = sur.spectra(test, jl, lall, kin, tol=args.surrogate_tol)
+    t_sur = time.perf_counter() - t1
+    den = [np.abs(judge[..., 0]), np.sqrt(np.abs(judge[..., 0] * judge[..., 2])), np.abs(judge[..., 2])]
+    rel = np.stack([np.max(np.abs(Dl[..., i] - judge[..., i]) / den[i], axis=1) for i in range(3)], axis=1)  # [cosmo][mode]
+    Dl_raw, _, _ = sur.spectra(test, jl, lall, kin, fallback=False)
+    rel_raw = np.stack([np.max(np.abs(Dl_raw[..., i] - judge[..., i]) / den[i], axis=1) for i in range(3)], axis=1)
+    n = len(test)
+    line = {"metric": "cosmologies/s (surrogate + fallback vs solver)", "value": round(n / t_sur, 3), "unit": "cosmologies/s",
+            "workload": f"{n} held-out cosmologies from the box, C_l TT/TE/EE to l={LMAX} (D_l), 400 k x 500 tau",
+            "solver_cosmologies_per_s": round(n / t_solver, 3), "speedup": round(t_solver / t_sur, 3),
+            "fallback_rate": float(fb.mean()), "tol_probe": args.surrogate_tol,
+            "probe_error": {"median": float(np.median(errs)), "max": float(np.max(errs))},
+            "cl_max_rel_vs_fp64": {"with_fallback": {"median": float(np.median(rel.max(axis=1))), "max": float(rel.max())},
+                                   "surrogate_only": {"median": float(np.median(rel_raw.max(axis=1))), "max": float(rel_raw.max())}},
+            "training": {"cosmologies": args.train_cosmologies, "samples": int(args.train_cosmologies * len(ks) * sur.ntau),
+                         "data_s": round(t_data, 2), "steps": steps, "train_s": round(t_train, 2),
+                         "tflops": round(steps * flops_step / t_train / 1e12, 1), "batch": 65536,
+                         "loss_first_last": [losses[0], losses[-1]], "mse_train_standardised": mse_train},
+            "model": "MLP 8 -> 4x512 SiLU -> 7 (perturbation factors), BF16 tcgen05 GEMMs, FP32 accumulate, Adam"}
+    print(json.dumps(line), flush=True)
+
+
 def profile_case(args):
     """Small cases for ncu section captures.  pt: 64 of the 1000 modes (even in log k, the slowest
     included), sources on 200 times.  los: one spectrum_cmb of the full workload (the line-of-sight
@@ -374,7 +442,11 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=("spectrum", "batched"), default="spectrum",
+    ap.add_argument("--train-cosmologies", type=int, default=64)
+    ap.add_argument("--train-seconds", type=float, default=120.0)
+    ap.add_argument("--test-cosmologies", type=int, default=16)
+    ap.add_argument("--surrogate-tol", type=float, default=0.05)
+    ap.add_argument("--workload", choices=("spectrum", "batched", "surrogate"), default="spectrum",
                     help="spectrum: the headline single-cosmology C_l workload; batched: 256 cosmologies, ragged k grids")
     ap.add_argument("--profile-case", choices=("pt", "los"), default=None,
                     help="small cases for ncu section captures (see profile_case)")
@@ -383,6 +455,8 @@ def main():
         profile_case(args)
     elif args.workload == "batched" and args.impl == "ours":
         run_batched(args)
+    elif args.workload == "surrogate" and args.impl == "ours":
+        run_surrogate(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

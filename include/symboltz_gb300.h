@@ -38,6 +38,9 @@ extern "C" {
 #define SBZ_OUT_STATE 2    /* full perturbation state at the saved times   (solvept output_func = identity) */
 #define SBZ_OUT_SOURCES4 3 /* k*S_T split into k*(SW + ISW), k*Doppler, k*polarisation, and k^2*S_E
                               (the four ST/SE terms of src/models/cosmologies.jl:99-104) */
+#define SBZ_OUT_FACTORS 4  /* the perturbation factors of the sources: δγ/4 + Ψ + Π/16, Ψ' + Φ', θb, θb',
+                              Π, Π', Π'' (S_T = v·f0 + e^{-κ} f1 + (v̇ f2 + v f3)/k² + 3(v̈ f4 + 2v̇ f5 + v f6)/(16k²),
+                              S_E = 3 v f4 / (16 (kχ)²)) */
 
 /* Cosmological parameters of one cosmology: parameters_Planck18 keys (src/parameters.jl:1-21). */
 typedef struct sbz_params {
@@ -104,7 +107,7 @@ int sbz_bg_coefficients(const sbz_problem* pb, int cosmo, int n, const double* t
  * has wavenumber ks[i] and initial time tau_ini[i] (clamped to the background span, src/solve.jl:527).
  * Saved times: taus[c*ntau + j] for cosmology c (saveat).  out layout:
  *   SBZ_OUT_SOURCES: out[(i*ntau + j)*3 + s]; SBZ_OUT_DELTA_M: out[i]; SBZ_OUT_STATE: out[(i*ntau + j)*n + m];
- *   SBZ_OUT_SOURCES4: out[(i*ntau + j)*4 + s].
+ *   SBZ_OUT_SOURCES4: out[(i*ntau + j)*4 + s]; SBZ_OUT_FACTORS: out[(i*ntau + j)*7 + s].
  * status[i] per mode (may be NULL); steps[2i], steps[2i+1] = accepted, rejected (may be NULL). */
 int sbz_solve_pt(sbz_problem* pb, int nk, const int* cosmo, const double* ks, const double* tau_ini,
                  int ntau, const double* taus, int output, double* out, int* status, int64_t* steps);

@@ -346,7 +346,7 @@ static int pt_run(sbz_problem* pb, int nk, const int* d_cosmo, const double* d_k
 static bool check_pt_args(sbz_problem* pb, int nk, int ntau, int output) {
   if (!pb || !pb->bg_done) { fail(SBZ_ERR_STATE, "call sbz_solve_bg first"); return false; }
   if (upload_tables(pb) != SBZ_OK) return false;
-  if (nk < 0 || ntau < 0 || output < SBZ_OUT_SOURCES || output > SBZ_OUT_SOURCES4) { fail(SBZ_ERR_ARG, "bad sizes or output"); return false; }
+  if (nk < 0 || ntau < 0 || output < SBZ_OUT_SOURCES || output > SBZ_OUT_FACTORS) { fail(SBZ_ERR_ARG, "bad sizes or output"); return false; }
   if (output != SBZ_OUT_DELTA_M && ntau == 0) { fail(SBZ_ERR_ARG, "saved times required"); return false; }
   return true;
 }
@@ -402,7 +402,8 @@ int sbz_solve_pt(sbz_problem* pb, int nk, const int* cosmo, const double* ks, co
   }
   const int n = pb->M.n;
   const size_t nout = output == SBZ_OUT_DELTA_M ? (size_t)nk : output == SBZ_OUT_SOURCES ? (size_t)nk * ntau * 3
-                      : output == SBZ_OUT_SOURCES4 ? (size_t)nk * ntau * 4 : (size_t)nk * ntau * n;
+                      : output == SBZ_OUT_SOURCES4 ? (size_t)nk * ntau * 4 : output == SBZ_OUT_FACTORS ? (size_t)nk * ntau * 7
+                      : (size_t)nk * ntau * n;
   // longest-first work order: high-k modes take the most steps
   std::vector<int> order(nk);
   std::iota(order.begin(), order.end(), 0);
@@ -454,7 +455,8 @@ int sbz_autotune_pt(sbz_problem* pb, int nk, const int* cosmo, const double* ks,
   }
   const int ns = (int)sk.size(), n = pb->M.n;
   const size_t nout = output == SBZ_OUT_DELTA_M ? (size_t)ns : output == SBZ_OUT_SOURCES ? (size_t)ns * ntau * 3
-                      : output == SBZ_OUT_SOURCES4 ? (size_t)ns * ntau * 4 : (size_t)ns * ntau * n;
+                      : output == SBZ_OUT_SOURCES4 ? (size_t)ns * ntau * 4 : output == SBZ_OUT_FACTORS ? (size_t)ns * ntau * 7
+                      : (size_t)ns * ntau * n;
   cudaStream_t s = pb->stream;
   SBZ_CUDA(pb->d_k.ensure(sizeof(double) * ns));
   SBZ_CUDA(pb->d_ti.ensure(sizeof(double) * ns));

@@ -1,5 +1,6 @@
 // Source surrogate: dense-layer GEMM launcher (tensor maps, tile choice) and C-ABI test entry.
 #include <cudaTypedefs.h>
+#include <algorithm>
 #include <cstdio>
 #include <mutex>
 #include "../../include/symboltz_gb300.h"
@@ -36,6 +37,16 @@ bool tmap_rows_k(CUtensorMap* tm, const void* ptr, int rows, int K, int box_rows
                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+int num_sms() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 1;
+  }
+  return n;
+}
+
 template <int BN>
 int launch(const GemmArgs& g, const void* A, const void* B, cudaStream_t st) {
   CUtensorMap ta, tb;
@@ -43,7 +54,21 @@ int launch(const GemmArgs& g, const void* A, const void* B, cudaStream_t st) {
   const size_t smem = gemm_smem_bytes<BN>();
   auto k = gemm_tn_kernel<BN>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return SBZ_ERR_CUDA;
-  const dim3 grid(g.N / BN, g.M / BM);
+  const int tiles = (g.N / BN) * (g.M / BM), KT = g.K / BK;
+  // weight gradients have few output tiles and a long K (the batch): split K over ~2 CTAs per SM,
+  // at least 4 K-steps each, and add the partial tiles atomically into a zeroed output
+  int splits = 1;
+  if (g.epi == EPI_F32 && tiles < num_sms()) splits = std::max(1, std::min(KT / 4, (2 * num_sms() + tiles - 1) / tiles));
+  if (splits > 1 && !g.accumulate) {
+    for (int r = 0; r < g.M; ++r) {  // rows of the output region (ldo may exceed N)
+      if (g.ldo == g.n_valid) {
+        if (cudaMemsetAsync(g.out_f32, 0, sizeof(float) * (size_t)g.M * g.ldo, st) != cudaSuccess) return SBZ_ERR_CUDA;
+        break;
+      }
+      if (cudaMemsetAsync(g.out_f32 + (size_t)r * g.ldo, 0, sizeof(float) * g.n_valid, st) != cudaSuccess) return SBZ_ERR_CUDA;
+    }
+  }
+  const dim3 grid(g.N / BN, g.M / BM, splits);
   k<<<grid, 128, smem, st>>>(ta, tb, g);
   return cudaGetLastError() == cudaSuccess ? SBZ_OK : SBZ_ERR_CUDA;
 }

@@ -7,7 +7,7 @@
 // tcgen05.mma (kind::f16, M = 128, N = BN, K = 16) into a TMEM accumulator and releases ring
 // slots with tcgen05.commit; all four warps then read the accumulator with tcgen05.ld (warp w owns
 // TMEM lanes 32w..32w+31 = tile rows) and apply the fused epilogue:
-//   EPI_F32   out_f32 = D (+ out_f32 when accumulate)                      weight gradients
+//   EPI_F32   out_f32 = D (+ out_f32 when accumulate; split-K CTAs add atomically) weight gradients
 //   EPI_ACT   z = D + bias; out = bf16(act(z)); optional z_out = bf16(z)    forward layers
 //   EPI_DACT  out = bf16(D · act'(z_in))                                   backward layers
 // Every mbarrier wait is bounded: a wait that runs out sets *err and the CTA skips ahead to its
@@ -114,7 +114,10 @@ __global__ void __launch_bounds__(128, 1) gemm_tn_kernel(const __grid_constant__
   uint32_t* tmem_slot = (uint32_t*)(done + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;
-  const int KT = g.K / BK;
+  // split-K (EPI_F32 only): CTA z owns K-steps [kt0, kt0 + KT) of the g.K / BK
+  const int KTall = g.K / BK;
+  const int kt0 = (int)((long long)KTall * blockIdx.z / gridDim.z);
+  const int KT = (int)((long long)KTall * (blockIdx.z + 1) / gridDim.z) - kt0;
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
     mbar_init(done, 1);
@@ -135,8 +138,8 @@ __global__ void __launch_bounds__(128, 1) gemm_tn_kernel(const __grid_constant__
       const uint32_t ph = (uint32_t)(kt / STAGES) & 1u;
       if (!mbar_wait(&empty[s], ph ^ 1u)) { ok = false; break; }
       mbar_expect_tx(&full[s], (unsigned)((BM + BN) * BK * 2));
-      tma_load_2d(sA + (size_t)s * BM * BK * 2, &tmA, kt * BK, m0, &full[s]);
-      tma_load_2d(sB + (size_t)s * BN * BK * 2, &tmB, kt * BK, n0, &full[s]);
+      tma_load_2d(sA + (size_t)s * BM * BK * 2, &tmA, (kt0 + kt) * BK, m0, &full[s]);
+      tma_load_2d(sB + (size_t)s * BN * BK * 2, &tmB, (kt0 + kt) * BK, n0, &full[s]);
     }
   } else if (warp == 1 && lane == 0) {  // MMA issuer
     const uint32_t idesc = idesc_bf16<BN>();
@@ -184,9 +187,13 @@ __global__ void __launch_bounds__(128, 1) gemm_tn_kernel(const __grid_constant__
       const int nv = min(32, g.n_valid - col);
       if (g.epi == EPI_F32) {
         float* out = g.out_f32 + o;
-        for (int j = 0; j < nv; ++j) {
-          const float d = __uint_as_float(v[j]);
-          out[j] = g.accumulate ? out[j] + d : d;
+        if (gridDim.z > 1) {
+          for (int j = 0; j < nv; ++j) atomicAdd(out + j, __uint_as_float(v[j]));
+        } else {
+          for (int j = 0; j < nv; ++j) {
+            const float d = __uint_as_float(v[j]);
+            out[j] = g.accumulate ? out[j] + d : d;
+          }
         }
       } else if (g.epi == EPI_ACT) {
         __align__(16) __nv_bfloat16 y[32], zz[32];

@@ -732,7 +732,7 @@ __device__ void emit_output(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const PtA
     for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) o[i] = y[sl]; }
     return;
   }
-  if (A.output != SBZ_OUT_SOURCES && A.output != SBZ_OUT_SOURCES4) return;
+  if (A.output != SBZ_OUT_SOURCES && A.output != SBZ_OUT_SOURCES4 && A.output != SBZ_OUT_FACTORS) return;
   // line-of-sight sources (src/models/cosmologies.jl:99-105)
   const int so = kNSets - 1;
   const double k = mk.k;
@@ -765,7 +765,11 @@ __device__ void emit_output(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const PtA
       const double sPol = 3.0 / 16.0 * mk.ik2 * (vdd * Pi + 2 * vd * Pid + v * Pidd);
       const double chi = cd->tau0 - tau;
       const double SE = 3.0 / 16.0 * v * Pi / ((k * chi) * (k * chi));
-      if (A.output == SBZ_OUT_SOURCES4) {
+      if (A.output == SBZ_OUT_FACTORS) {
+        double* o = A.out + ((size_t)item * A.ntau + j) * 7;
+        o[0] = W.x[5] * 0.25 + psi + Pi / 16; o[1] = psid + phid; o[2] = W.x[4]; o[3] = W.f[4];
+        o[4] = Pi; o[5] = Pid; o[6] = Pidd;
+      } else if (A.output == SBZ_OUT_SOURCES4) {
         double* o = A.out + ((size_t)item * A.ntau + j) * 4;
         o[0] = k * (sSW + sISW); o[1] = k * sDop; o[2] = k * sPol; o[3] = k * k * SE;
       } else {
@@ -890,7 +894,10 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         if (taus[jout] < t) {  // before the mode starts: zero
           if (A.output == SBZ_OUT_SOURCES && gt < 3) A.out[((size_t)item * A.ntau + jout) * 3 + gt] = 0;
         if (A.output == SBZ_OUT_SOURCES4 && gt < 4) A.out[((size_t)item * A.ntau + jout) * 4 + gt] = 0;
+        if (A.output == SBZ_OUT_FACTORS && gt < 7) A.out[((size_t)item * A.ntau + jout) * 7 + gt] = 0;
           if (A.output == SBZ_OUT_SOURCES4 && gt < 4) A.out[((size_t)item * A.ntau + jout) * 4 + gt] = 0;
+        if (A.output == SBZ_OUT_FACTORS && gt < 7) A.out[((size_t)item * A.ntau + jout) * 7 + gt] = 0;
+          if (A.output == SBZ_OUT_FACTORS && gt < 7) A.out[((size_t)item * A.ntau + jout) * 7 + gt] = 0;
           if (A.output == SBZ_OUT_STATE) for (int i = gt; i < n; i += NT) A.out[((size_t)item * A.ntau + jout) * n + i] = 0;
         } else {
           emit_output(g, W, A, cd, tab, comps, M, mk, t, y, item, jout);
@@ -1104,6 +1111,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
       for (; jout < A.ntau; ++jout) {
         if (A.output == SBZ_OUT_SOURCES && gt < 3) A.out[((size_t)item * A.ntau + jout) * 3 + gt] = 0;
         if (A.output == SBZ_OUT_SOURCES4 && gt < 4) A.out[((size_t)item * A.ntau + jout) * 4 + gt] = 0;
+        if (A.output == SBZ_OUT_FACTORS && gt < 7) A.out[((size_t)item * A.ntau + jout) * 7 + gt] = 0;
         if (A.output == SBZ_OUT_STATE) for (int i = gt; i < n; i += NT) A.out[((size_t)item * A.ntau + jout) * n + i] = 0;
       }
     }

@@ -175,7 +175,7 @@ def solvebg(prob: CosmologyProblem):
     return prob.solvebg()
 
 
-_OUT = {"sources": L.SBZ_OUT_SOURCES, "delta_m": L.SBZ_OUT_DELTA_M, "state": L.SBZ_OUT_STATE, "sources4": L.SBZ_OUT_SOURCES4}
+_OUT = {"sources": L.SBZ_OUT_SOURCES, "delta_m": L.SBZ_OUT_DELTA_M, "state": L.SBZ_OUT_STATE, "sources4": L.SBZ_OUT_SOURCES4, "factors": L.SBZ_OUT_FACTORS}
 
 
 def autotune(prob: CosmologyProblem, ks, ptivini=-np.inf, *, saveat=None, output="sources", cosmo=None):
@@ -226,7 +226,7 @@ def solvept(prob: CosmologyProblem, ks, ptivini=-np.inf, *, saveat=None, output=
         taus = np.broadcast_to(taus, (prob.ncosmo, taus.shape[-1])) if taus.ndim == 1 else taus
     taus = L.f64(taus)
     ntau = taus.shape[1]
-    shape = {L.SBZ_OUT_DELTA_M: (nk,), L.SBZ_OUT_SOURCES: (nk, ntau, 3), L.SBZ_OUT_SOURCES4: (nk, ntau, 4),
+    shape = {L.SBZ_OUT_DELTA_M: (nk,), L.SBZ_OUT_SOURCES: (nk, ntau, 3), L.SBZ_OUT_SOURCES4: (nk, ntau, 4), L.SBZ_OUT_FACTORS: (nk, ntau, 7),
              L.SBZ_OUT_STATE: (nk, ntau, prob.nstate)}[kind]
     out = np.zeros(shape)
     st = np.zeros(nk, dtype=np.int32)

@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(PKG, "lib", "libsymboltz_gb300.so")
 SBZ_OK, SBZ_MAXITERS, SBZ_DTMIN, SBZ_NONFINITE = 0, 1, 2, 3
 SBZ_ERR_ARG, SBZ_ERR_CUDA, SBZ_ERR_NOMEM, SBZ_ERR_STATE = -1, -2, -3, -4
 SBZ_FP64, SBZ_MIXED = 0, 1
-SBZ_OUT_SOURCES, SBZ_OUT_DELTA_M, SBZ_OUT_STATE, SBZ_OUT_SOURCES4 = 0, 1, 2, 3
+SBZ_OUT_SOURCES, SBZ_OUT_DELTA_M, SBZ_OUT_STATE, SBZ_OUT_SOURCES4, SBZ_OUT_FACTORS = 0, 1, 2, 3, 4
 
 EXPORTS = (
     "sbz_default_opts", "sbz_last_error", "sbz_momentum_quadrature", "sbz_problem_create", "sbz_problem_destroy",

@@ -1,9 +1,10 @@
 """Learned source surrogate with solver fallback.
 
-An MLP maps (six cosmological parameters, log k, log τ) to the four line-of-sight source terms
-(k(S_SW + S_ISW), k S_Doppler, k S_polarisation, k² S_E; src/models/cosmologies.jl:99-104).  It is
-trained on sources computed by the GPU perturbation solver (output "sources4") with the library's
-own BF16 tensor-core forward/backward kernels (``sbz_surrogate_*``), and evaluated the same way.
+An MLP maps (six cosmological parameters, log k, log τ) to the smooth perturbation factors of the
+line-of-sight sources (src/models/cosmologies.jl:99-104); the sources follow exactly from them and
+each cosmology's visibility function.  It is trained on factors computed by the GPU perturbation
+solver (output "factors") with the library's own BF16 tensor-core forward/backward kernels
+(``sbz_surrogate_*``), and evaluated the same way.
 Its sources go through the regular k-interpolation → line-of-sight → C_ℓ pipeline
 (``sbz_spectrum_cmb_sources``).  Each cosmology gets an error estimate from a few probe modes that
 are also solved with the real solver; a cosmology whose probes disagree by more than the tolerance is
@@ -115,34 +116,63 @@ def cmb_taus(bg_t, tau0, ntau):
 
 
 class SourceSurrogate:
-    """Sources on a fixed coarse k grid and per-cosmology τ grids, learned by an MLP.
+    """Line-of-sight sources on a fixed coarse k grid and per-cosmology τ grids, from an MLP of the
+    seven perturbation factors the sources are built from (f0 = δγ/4 + Ψ + Π/16, f1 = Ψ' + Φ',
+    f2 = θb, f3 = θb', f4 = Π, f5 = Π', f6 = Π''; solver output "factors").  The sharp recombination
+    structure lives in the visibility v and its derivatives, which come exactly from each cosmology's
+    background; the network learns the smooth factors, scaled by powers of k and, except the ISW
+    factor, tapered by the normalised visibility envelope (so the loss ignores times the sources never
+    see).  Sources: k S_T = k [v f0 + e^{-κ} f1 + (v̇ f2 + v f3)/k² + 3 (v̈ f4 + 2 v̇ f5 + v f6)/(16 k²)],
+    k² S_E = 3 v f4 / (16 χ²)  (src/models/cosmologies.jl:99-104)."""
 
-    ks: coarse k grid (H0/c) shared by all cosmologies; ntau: times per cosmology."""
+    KPOW = np.array([0, 0, 1, 2, 0, 1, 2])  # factors are learned as f_j / k^KPOW[j]
 
     def __init__(self, M, ks, ntau=500, width=512, nhidden=4, batch=65536, seed=0):
         self.M, self.ks, self.ntau = M, np.asarray(ks, dtype=np.float64), ntau
         self.logk = (np.log(self.ks.min()), np.log(self.ks.max()))
-        self.net = MLP(8, width, nhidden, 4, batch, seed)
-        self.mean = np.zeros(4)
-        self.scale = np.ones(4)
+        self.net = MLP(8, width, nhidden, 7, batch, seed)
+        self.mean = np.zeros(7)
+        self.scale = np.ones(7)
 
-    # ---- features and targets -------------------------------------------------------------
-    def features(self, theta, taus):
+    # ---- features, background, targets ------------------------------------------------------
+    def features(self, theta, taus, ks=None):
         """[nk * ntau, 8] inputs for one cosmology: θ mapped to [-1, 1] by the box, log k and log τ to
         [-1, 1]; row i*ntau + j is (k_i, τ_j)."""
+        ks = self.ks if ks is None else np.asarray(ks, dtype=np.float64)
         th = 2 * (np.asarray(theta) - BOX[:, 0]) / (BOX[:, 1] - BOX[:, 0]) - 1
-        lk = 2 * (np.log(self.ks) - self.logk[0]) / (self.logk[1] - self.logk[0]) - 1
+        lk = 2 * (np.log(ks) - self.logk[0]) / (self.logk[1] - self.logk[0]) - 1
         lt = 2 * (np.log(taus) - LOGTAU[0]) / (LOGTAU[1] - LOGTAU[0]) - 1
-        nk, nt = len(self.ks), len(taus)
+        nk, nt = len(ks), len(taus)
         X = np.empty((nk * nt, 8), dtype=np.float32)
         X[:, :6] = th
         X[:, 6] = np.repeat(lk, nt)
         X[:, 7] = np.tile(lt, nk)
         return X
 
-    def solve_sources(self, thetas, precision="mixed", ks=None):
-        """Solver sources4 for each θ on (ks or the coarse grid) × its own τ grid:
-        returns (sources [ncos][nk][ntau][4], taus [ncos][ntau], envelopes [ncos][ntau], problem)."""
+    @staticmethod
+    def visibility(coef):
+        """v, v̇, v̈, e^{-κ} from the GPU coefficient columns (a, ℋ, κ̇, c_s², e^{-κ}, κ̈, κ⃛), the
+        same expressions the perturbation kernel evaluates."""
+        kd, ek, kdd, kddd = coef[:, 2], coef[:, 4], coef[:, 5], coef[:, 6]
+        v = -kd * ek
+        vd = (kd * kd - kdd) * ek
+        vdd = (-kd * kd * kd + 3 * kd * kdd - kddd) * ek
+        return np.stack([v, vd, vdd, ek])
+
+    @staticmethod
+    def taper(vis):
+        """Normalised visibility envelope (|v| + a|v̇| + b|v̈|)/max ∈ [0, 1]: zero where no source
+        term sees the visibility-carried factors (before recombination), so their stiff early-time
+        transients do not enter the loss."""
+        v, vd, vdd = np.abs(vis[0]), np.abs(vis[1]), np.abs(vis[2])
+        d1 = v.max() / max(vd.max(), 1e-300)
+        d2 = v.max() / max(vdd.max(), 1e-300)
+        t = v + d1 * vd + d2 * vdd
+        return t / t.max()
+
+    def solve_factors(self, thetas, precision="mixed", ks=None):
+        """Solver factors [ncos][nk][ntau][7] on (ks or the coarse grid) × each cosmology's τ grid,
+        with taus [ncos][ntau], visibilities [ncos][4][ntau] and the problem."""
         from . import CosmologyProblem, solvept
         ks = self.ks if ks is None else np.asarray(ks, dtype=np.float64)
         prob = CosmologyProblem(self.M, [box_params(t) for t in thetas], precision=precision)
@@ -152,46 +182,48 @@ class SourceSurrogate:
         taus = np.stack([cmb_taus(bg.t(c), bg.tau0[c], self.ntau) for c in range(len(thetas))])
         nk = len(ks)
         cos = np.repeat(np.arange(len(thetas)), nk)
-        out, st, _ = solvept(prob, np.tile(ks, len(thetas)), prob.opts.tau_ini, saveat=taus, output="sources4", cosmo=cos)
+        out, st, _ = solvept(prob, np.tile(ks, len(thetas)), prob.opts.tau_ini, saveat=taus, output="factors", cosmo=cos)
         if np.any(st != 0):
-            raise L.SbzError(f"{int(np.count_nonzero(st))} training modes failed")
-        out = out.reshape(len(thetas), nk, self.ntau, 4)
-        out[:, :, -1, :] = 0.0  # χ = 0: zeroed, as the line of sight does (src/observables/angular.jl:296)
-        env = np.stack([self.envelope(bg.eval(taus[c], c)) for c in range(len(thetas))])
-        return out, taus, env, prob
+            raise L.SbzError(f"{int(np.count_nonzero(st))} modes failed")
+        vis = np.stack([self.visibility(bg.coefficients(taus[c], c)) for c in range(len(thetas))])
+        return out.reshape(len(thetas), nk, self.ntau, 7), taus, vis, prob
+
+    def weights(self, vis):
+        """Per-time multipliers of the learned factors: the visibility envelope for f0, f2..f6 and
+        e^{-κ} for the ISW factor f1."""
+        w = np.repeat(self.taper(vis)[:, None], 7, axis=1)
+        w[:, 1] = vis[3]
+        return w
+
+    def to_targets(self, F, ks, vis):
+        with np.errstate(over="ignore", invalid="ignore"):
+            G = F / ks[:, None, None] ** self.KPOW * self.weights(vis)[None]
+        return np.where(self.weights(vis)[None] > 0, G, 0.0)
+
+    def from_targets(self, G, ks, vis):
+        w = self.weights(vis)[None]
+        F = np.where(w > 1e-12, G / np.where(w > 1e-12, w, 1.0), 0.0)  # sources there carry v ≈ 0 or e^{-κ} ≈ 0
+        return F * ks[:, None, None] ** self.KPOW
 
     @staticmethod
-    def envelope(bgv):
-        """|v| + e^{-κ} + 1e-3 max|v| from background columns (…, κ, v, …): the visibility and
-        transparency factors the sources carry, so that sources / envelope are smooth in τ."""
-        v, kappa = bgv[:, 4], bgv[:, 3]
-        return np.abs(v) + np.exp(-kappa) + 1e-3 * np.max(np.abs(v))
-
-    @staticmethod
-    def _chi2(taus):
-        return (taus[-1] - taus) ** 2  # χ² = (τ0 - τ)²
-
-    def to_targets(self, S4, taus, env):
-        """Learned quantities for sources4 [nk][ntau][4] on one cosmology's τ grid: the three
-        temperature terms and χ² k² S_E = (3/16) v Π (removing the 1/χ² of S_E), each divided by the
-        cosmology's visibility envelope (the sharp recombination peak is known exactly from the
-        background; the network learns the smooth factors multiplying it)."""
-        Y = S4.copy()
-        Y[..., 3] *= self._chi2(taus)
-        return Y / env[None, :, None]
-
-    def from_targets(self, Y, taus, env):
-        S4 = Y * env[None, :, None]
-        chi2 = self._chi2(taus)
-        S4[..., 3] = np.where(chi2 > 0, S4[..., 3] / np.where(chi2 > 0, chi2, 1.0), 0.0)
-        S4[:, -1, :] = 0.0
-        return S4
+    def sources(F, ks, taus, vis):
+        """(k S_T, k² S_E, S_ψ = 0) [nk][ntau][3] from factors; zero at χ = 0 (angular.jl:296)."""
+        v, vd, vdd, ek = (x[None, :] for x in vis)
+        k = ks[:, None]
+        f = [F[..., j] for j in range(7)]
+        sT = v * f[0] + ek * f[1] + (vd * f[2] + v * f[3]) / k**2 + 3.0 / (16.0 * k**2) * (vdd * f[4] + 2 * vd * f[5] + v * f[6])
+        chi2 = (taus[-1] - taus)[None, :] ** 2
+        out = np.zeros(F.shape[:2] + (3,))
+        out[..., 0] = k * sT
+        out[..., 1] = np.where(chi2 > 0, 3.0 / 16.0 * v * f[4] / np.where(chi2 > 0, chi2, 1.0), 0.0)
+        out[:, -1, :] = 0.0
+        return out
 
     def dataset(self, thetas):
         """(X, Y, taus) training arrays from the solver for the given parameter points."""
-        S, taus, env, _ = self.solve_sources(thetas)
+        F, taus, vis, _ = self.solve_factors(thetas)
         X = np.concatenate([self.features(t, taus[c]) for c, t in enumerate(thetas)])
-        Y = np.concatenate([self.to_targets(S[c], taus[c], env[c]).reshape(-1, 4) for c in range(len(thetas))])
+        Y = np.concatenate([self.to_targets(F[c], self.ks, vis[c]).reshape(-1, 7) for c in range(len(thetas))])
         return X, Y, taus
 
     # ---- training ---------------------------------------------------------------------------
@@ -217,44 +249,34 @@ class SourceSurrogate:
         return float(np.mean((P - (Y - self.mean) / self.scale) ** 2))
 
     # ---- prediction ------------------------------------------------------------------------
-    def predict(self, theta, taus, env, ks=None):
-        """Sources4 [nk][ntau][4] for one cosmology (physical units); env: its visibility envelope."""
-        if ks is not None:
-            keep, self.ks = self.ks, np.asarray(ks, dtype=np.float64)
-            try:
-                X = self.features(theta, taus)
-            finally:
-                self.ks = keep
-        else:
-            X = self.features(theta, taus)
-        Y = (self.net.infer(X).astype(np.float64) * self.scale + self.mean).reshape(-1, len(taus), 4)
-        return self.from_targets(Y, taus, env)
+    def predict_factors(self, theta, taus, vis, ks=None):
+        ks = self.ks if ks is None else np.asarray(ks, dtype=np.float64)
+        G = (self.net.infer(self.features(theta, taus, ks)).astype(np.float64) * self.scale + self.mean).reshape(len(ks), len(taus), 7)
+        return self.from_targets(G, ks, vis)
 
-    @staticmethod
-    def los_sources(S4):
-        """(k S_T, k² S_E, S_ψ = 0) in the layout of the line-of-sight pipeline."""
-        out = np.zeros(S4.shape[:2] + (3,))
-        out[..., 0] = S4[..., 0] + S4[..., 1] + S4[..., 2]
-        out[..., 1] = S4[..., 3]
-        return out
+    def predict_sources(self, theta, taus, vis, ks=None):
+        ks = self.ks if ks is None else np.asarray(ks, dtype=np.float64)
+        return self.sources(self.predict_factors(theta, taus, vis, ks), ks, taus, vis)
 
     def save(self, path):
         self.net.save(path)
         np.savez(str(path) + ".norm.npz", mean=self.mean, scale=self.scale, ks=self.ks, ntau=self.ntau)
 
-    def probe_error(self, theta, taus, env, S4_true, kprobe):
-        """Relative L2 error of the predicted sources against solver sources at the probe modes."""
-        P = self.predict(theta, taus, env, ks=kprobe)
-        return float(np.linalg.norm(P - S4_true) / (np.linalg.norm(S4_true) + 1e-300))
+    def probe_error(self, theta, taus, vis, F_true, kprobe):
+        """Relative L2 error of the predicted sources (k S_T, k² S_E) against the solver's at the
+        probe modes."""
+        P = self.predict_sources(theta, taus, vis, kprobe)[..., :2]
+        T = self.sources(F_true, kprobe, taus, vis)[..., :2]
+        return float(np.linalg.norm(P - T) / (np.linalg.norm(T) + 1e-300))
 
     def spectra(self, thetas, jl, ls_out, kinterp, modes=("TT", "TE", "EE"), tol=0.05, kprobe=None, fallback=True):
-        """C_ℓ for each θ: surrogate sources through the line-of-sight pipeline, or the solver for
-        cosmologies whose probe-mode error exceeds tol.  Returns (Dl [ncos][nl][nmodes],
-        probe errors, fallback mask)."""
+        """C_ℓ (D_ℓ) for each θ: surrogate sources through the line-of-sight pipeline, or the solver
+        for cosmologies whose probe-mode error exceeds tol.  Returns (Dl [ncos][nl][nmodes], probe
+        errors, fallback mask)."""
         from . import CosmologyProblem, spectrum_cmb
         kprobe = np.geomspace(self.ks.min() * 10, self.ks.max() / 3, 4) if kprobe is None else np.asarray(kprobe)
-        S4p, taus, env, prob = self.solve_sources(thetas, ks=kprobe)
-        errs = np.array([self.probe_error(t, taus[c], env[c], S4p[c], kprobe) for c, t in enumerate(thetas)])
+        Fp, taus, vis, prob = self.solve_factors(thetas, ks=kprobe)
+        errs = np.array([self.probe_error(t, taus[c], vis[c], Fp[c], kprobe) for c, t in enumerate(thetas)])
         fb = (errs > tol) if fallback else np.zeros(len(thetas), dtype=bool)
         out = []
         for c, t in enumerate(thetas):
@@ -262,7 +284,7 @@ class SourceSurrogate:
                 p1 = CosmologyProblem(self.M, box_params(t))
                 out.append(spectrum_cmb(list(modes), p1, jl, ls_out, kinterp=kinterp, taus=taus[c], normalization="Dl"))
             else:
-                src = self.los_sources(self.predict(t, taus[c], env[c], ks=kinterp.xs))
+                src = self.predict_sources(t, taus[c], vis[c], ks=kinterp.xs)
                 out.append(spectrum_cmb(list(modes), prob, jl, ls_out, kinterp=kinterp, taus=taus[c], cosmo=c, normalization="Dl",
                                         sources=src))
         return np.stack(out), errs, fb

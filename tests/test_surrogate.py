@@ -81,7 +81,7 @@ def test_surrogate_sources_through_the_line_of_sight_with_fallback():
     sur = SourceSurrogate(M, ks, ntau=48, width=128, nhidden=2, batch=1024, seed=3)
     train = sample_box(4, seed=0)
     X, Y, _ = sur.dataset(train)
-    assert X.shape == (4 * 32 * 48, 8) and np.all(np.isfinite(Y))
+    assert X.shape == (4 * 32 * 48, 8) and Y.shape == (4 * 32 * 48, 7) and np.all(np.isfinite(Y))
     sur.fit(X, Y, steps=1, lr=1e-4)
     before = sur.mse(X, Y)
     sur.fit(X, Y, steps=400, lr=2e-3, lr_final=2e-4, chunks=4)
@@ -95,7 +95,25 @@ def test_surrogate_sources_through_the_line_of_sight_with_fallback():
     Dfb, err2, fb2 = sur.spectra(test, jl, ls, kin, tol=0.0)
     assert fb2.all()
     np.testing.assert_allclose(err2, err)
-    _, taus, _, _ = sur.solve_sources(test[:1])
+    _, taus, _, _ = sur.solve_factors(test[:1])
     ref = S.spectrum_cmb(["TT", "TE", "EE"], S.CosmologyProblem(M, box_params(test[0])), jl, ls, kinterp=kin, taus=taus[0],
                          normalization="Dl")
     np.testing.assert_allclose(Dfb[0], ref, rtol=1e-12)
+
+
+def test_factors_rebuild_the_solver_sources():
+    """Sources assembled from the solver's factors and the background visibility equal the solver's
+    own sources (same operator, same coefficient table)."""
+    import symboltz as S
+    from symboltz.surrogate import SourceSurrogate, sample_box
+    M = S.ΛCDM(lmax=5)
+    ks = S.k_from_hMpc(S.loggrid(1e-4, 0.3, length=16))
+    sur = SourceSurrogate(M, ks, ntau=40, width=128, nhidden=1, batch=128)
+    F, taus, vis, prob = sur.solve_factors(sample_box(1, seed=5))
+    rebuilt = sur.sources(F[0], ks, taus[0], vis[0])
+    direct, st, _ = S.solvept(prob, ks, prob.opts.tau_ini, saveat=taus[0], output="sources")
+    assert np.all(st == 0)
+    direct[:, -1, :] = 0.0
+    for s in range(2):
+        scale = np.max(np.abs(direct[..., s]))
+        np.testing.assert_allclose(rebuilt[..., s], direct[..., s], rtol=0, atol=1e-9 * scale)
