@@ -33,6 +33,11 @@ PARAMS = dict(h=H_PLANCK, Omega_c=0.12 / H_PLANCK**2, Omega_b=0.022 / H_PLANCK**
 MODEL = dict(lmax_gamma=30, lmax_nu=10, lmax_h=10, nx=5)
 NK, NTAU, LMAX = 1000, 2000, 2500
 METRIC = "k-mode solves/s (cosmologies/s) at <=1e-4 rel C_l err"
+# Lazy refinement threshold for the C_l workload: stages 2-6 skip the FP64 refinement when stage 1's
+# first correction is below 1e-4 of the error weights.  The C_l it gives agree with the fully
+# refined solve (the accuracy field below compares every run against all-FP64); pointwise sources
+# would want the library default 1e-5.
+REFINE_SKIP_CL = 1e-4
 
 
 def workload_grids(S, prob):
@@ -138,7 +143,7 @@ def run_ours(args):
         dist.init_process_group("nccl")
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
     M = S.ΛCDM(lmax_gamma=MODEL["lmax_gamma"], lmax_nu=MODEL["lmax_nu"], lmax_h=MODEL["lmax_h"], nx=MODEL["nx"])
-    prob = S.CosmologyProblem(M, PARAMS, precision=args.precision)
+    prob = S.CosmologyProblem(M, PARAMS, precision=args.precision, refine_skip=REFINE_SKIP_CL)
     ks, taus, ls = workload_grids(S, prob)
     jl = S.SphericalBesselCache(ls)
     kinterp = S.CubicSplineInterpolator(ks, f=np.log)
@@ -213,7 +218,8 @@ def run_ours(args):
         "data": "synthetic (fixed cosmological parameters)",
         "config": {"workload": "LCDM+massive-nu, l_gamma=30, 1000 k log 1e-5..5 h/Mpc, 2000 tau, TT/TE/EE to l=2500",
                    "n_state": prob.nstate, "nk": NK, "ntau": NTAU, "nl_sampled": int(len(ls)), "nk_fine": nk_fine,
-                   "precision": args.precision, "pt_rtol": prob.opts.pt_rtol, "l2": "flushed (256 MB write) between steps"},
+                   "precision": args.precision, "pt_rtol": prob.opts.pt_rtol, "refine_skip": REFINE_SKIP_CL,
+                   "l2": "flushed (256 MB write) between steps"},
         "cosmologies_per_s": round(world * K / (dev / 1e3), 4),
         "e2e": {"value": round(e2e_v, 2), "unit": "k-modes/s", "cosmologies_per_s": round(world * K / (e2e / 1e3), 4),
                 "h2d_bytes_per_step": int(8 * (3 * NK + 2 * NTAU + 2 * len(ls))), "d2h_bytes_per_step": int(8 * 3 * len(ls) + 4 * NK)},

@@ -146,7 +146,7 @@ void sbz_default_opts(sbz_opts* o) {
   o->bg_rtol = 1e-7; o->bg_atol = 1e-7; o->pt_rtol = 1e-5; o->pt_atol = 1e-5;
   o->tau_ini = 1e-6; o->tau_max = 100.0; o->maxiters = 100000;
   o->precision = SBZ_MIXED; o->refine_iters = 3; o->table_points = 8192; o->warps_per_block = 0; o->warps_per_mode = 0; o->blocks_per_sm = 0;
-  o->los_precision = -1;
+  o->los_precision = -1; o->refine_skip = 1e-5;
 }
 
 const char* sbz_last_error(void) { return g_err.c_str(); }
@@ -336,6 +336,7 @@ static int pt_run(sbz_problem* pb, int nk, const int* d_cosmo, const double* d_k
   A.output = output; A.out = d_out; A.status = d_status; A.steps = d_steps;
   A.rtol = pb->opts.pt_rtol; A.atol = pb->opts.pt_atol; A.maxiters = pb->opts.maxiters;
   A.refine = pb->opts.precision == SBZ_MIXED ? std::max(0, pb->opts.refine_iters) : 0;
+  A.refine_skip = (float)pb->opts.refine_skip;
   A.counter = pb->d_counter.as<unsigned>();
   SBZ_CUDA(cudaMemsetAsync(A.counter, 0, sizeof(unsigned), pb->stream));
   const int r = sbz::pt_launch(A, pb->opts.precision, pb->opts.warps_per_block, pb->opts.warps_per_mode, pb->opts.blocks_per_sm, pb->num_sms, pb->stream);
@@ -650,6 +651,7 @@ static int spectrum_cmb_impl(sbz_problem* pb, int cosmo, const sbz_bessel* jl, i
     A.out = pb->d_out.as<double>(); A.status = pb->d_status.as<int>(); A.steps = pb->d_steps.as<int64_t>();
     A.rtol = pb->opts.pt_rtol; A.atol = pb->opts.pt_atol; A.maxiters = pb->opts.maxiters;
     A.refine = pb->opts.precision == SBZ_MIXED ? std::max(0, pb->opts.refine_iters) : 0;
+  A.refine_skip = (float)pb->opts.refine_skip;
     A.counter = pb->d_counter.as<unsigned>();
     SBZ_CUDA(cudaMemsetAsync(A.counter, 0, sizeof(unsigned), st));
     r = sbz::pt_launch(A, pb->opts.precision, pb->opts.warps_per_block, pb->opts.warps_per_mode, pb->opts.blocks_per_sm, pb->num_sms, st);

@@ -688,7 +688,8 @@ __device__ __forceinline__ void solve_W(const Grp<NW>& g, ModeMem<NW, NSL, ST>& 
 template <int NW, int NSL, typename ST>
 __device__ __forceinline__ void stage_solve(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const Factor<ST>& F, const CSet& CJ,
                             const CompDesc* __restrict__ comps, const ModelDesc& M, double k, double s, int refine,
-                            bool scan, const float (&isk)[NSL], const double (&b)[NSL], double (&U)[NSL]) {
+                            bool scan, const float (&isk)[NSL], const double (&b)[NSL], double (&U)[NSL],
+                            float* first_correction = nullptr) {
   const int gt = g.gt;
 #pragma unroll
   for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) W.r[i] = (ST)b[sl]; }
@@ -715,7 +716,11 @@ __device__ __forceinline__ void stage_solve(const Grp<NW>& g, ModeMem<NW, NSL, S
       const int i = comp_of<NW>(gt, sl);
       if (i < M.n) { const ST d = W.u[i]; U[sl] += (double)d; c = fmaxf(c, fabsf((float)d) * isk[sl]); }
     }
-    if (it + 1 < refine && group_max(g, W, c) < 1e-3f) break;
+    if (it + 1 < refine || (it == 0 && first_correction)) {
+      const float cm = group_max(g, W, c);
+      if (it == 0 && first_correction) *first_correction = cm;
+      if (it + 1 < refine && cm < 1e-3f) break;
+    }
   }
 }
 
@@ -979,7 +984,11 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         for (int sl = 0; sl < NSL; ++sl) isk[sl] = 1.0f / (float)(atol + rtol * fabs(y[sl]));
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = f0[sl] + h * rw::d1 * ft[sl];
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, isk, b, U1);
+        float c1 = 1e30f;
+        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, isk, b, U1, &c1);
+        // lazy refinement: stages 2-6 share stage 1's W; when its first FP64 correction is already
+        // below refine_skip (error-weight units) the FP32 solves are accurate and are not refined
+        const int rk = (A.refine > 0 && c1 < A.refine_skip) ? 0 : A.refine;
         // stage 2
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl] + rw::A21 * U1[sl]; }
@@ -987,7 +996,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         matvec<NW, NSL>(gt, W.x, W.cs[s2], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C21 * U1[sl]) + h * rw::d2 * ft[sl];
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, isk, b, U2);
+        stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U2);
         // stage 3
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl] + rw::A31 * U1[sl] + rw::A32 * U2[sl]; }
@@ -995,7 +1004,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         matvec<NW, NSL>(gt, W.x, W.cs[s3], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C31 * U1[sl] + rw::C32 * U2[sl]) + h * rw::d3 * ft[sl];
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, isk, b, U3);
+        stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U3);
         // stage 4
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl] + rw::A41 * U1[sl] + rw::A42 * U2[sl] + rw::A43 * U3[sl]; }
@@ -1003,7 +1012,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         matvec<NW, NSL>(gt, W.x, W.cs[s4], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C41 * U1[sl] + rw::C42 * U2[sl] + rw::C43 * U3[sl]) + h * rw::d4 * ft[sl];
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, isk, b, U4);
+        stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U4);
         // stage 5 (at t + h)
         double Y[NSL];
 #pragma unroll
@@ -1016,7 +1025,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         matvec<NW, NSL>(gt, W.x, W.cs[s5], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C51 * U1[sl] + rw::C52 * U2[sl] + rw::C53 * U3[sl] + rw::C54 * U4[sl]);
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, isk, b, U5);
+        stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U5);
         // stage 6
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); Y[sl] += U5[sl]; if (i < n) W.x[i] = Y[sl]; }
@@ -1024,7 +1033,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         matvec<NW, NSL>(gt, W.x, W.cs[s5], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C61 * U1[sl] + rw::C62 * U2[sl] + rw::C63 * U3[sl] + rw::C64 * U4[sl] + rw::C65 * U5[sl]);
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, isk, b, U6);
+        stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U6);
         // error estimate and new state (the norm only steers the step size: FP32 in mixed mode)
         double y1[NSL], err2;
         if constexpr (sizeof(ST) == 4) {

@@ -100,7 +100,7 @@ class CosmologyProblem:
 
     def __init__(self, M: Model, pars, *, bg_rtol=1e-7, bg_atol=1e-7, pt_rtol=1e-5, pt_atol=1e-5, ivspan=(1e-6, 100.0),
                  maxiters=100000, precision="mixed", refine_iters=3, table_points=8192, warps_per_block=0,
-                 warps_per_mode=0, blocks_per_sm=0, los_precision=None):
+                 warps_per_mode=0, blocks_per_sm=0, los_precision=None, refine_skip=None):
         self.M = M
         self.pars = [dict(p) for p in ([pars] if isinstance(pars, dict) else pars)]
         o = L.Opts()
@@ -112,6 +112,8 @@ class CosmologyProblem:
         o.refine_iters, o.table_points, o.warps_per_block = refine_iters, table_points, warps_per_block
         o.warps_per_mode, o.blocks_per_sm = warps_per_mode, blocks_per_sm
         o.los_precision = -1 if los_precision is None else {"fp64": L.SBZ_FP64, "mixed": L.SBZ_MIXED}[los_precision]
+        if refine_skip is not None:
+            o.refine_skip = refine_skip
         self.opts = o
         self._m = M.c()
         pc, n = _params_c(self.pars)

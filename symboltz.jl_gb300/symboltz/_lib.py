@@ -43,7 +43,7 @@ class Opts(C.Structure):
                 ("tau_ini", C.c_double), ("tau_max", C.c_double), ("maxiters", C.c_int64), ("precision", C.c_int),
                 ("refine_iters", C.c_int), ("table_points", C.c_int), ("warps_per_block", C.c_int),
                 ("warps_per_mode", C.c_int), ("blocks_per_sm", C.c_int),
-                ("los_precision", C.c_int)]
+                ("los_precision", C.c_int), ("refine_skip", C.c_double)]
 
 
 class SbzError(RuntimeError):
