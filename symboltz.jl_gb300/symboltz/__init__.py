@@ -238,6 +238,77 @@ def solvept(prob: CosmologyProblem, ks, ptivini=-np.inf, *, saveat=None, output=
     return out, st, steps
 
 
+def _isapprox(x, y, atol, rtol, norm):
+    """Julia's isapprox for arrays: norm(x - y) <= max(atol, rtol * max(norm(x), norm(y)))."""
+    return norm(x - y) <= max(atol, rtol * max(norm(x), norm(y)))
+
+
+def refine_grid(fun, ks, *, atol=0.0, rtol=None, norm=np.linalg.norm, ktransform=(lambda k: k, lambda k: k), maxks=1024,
+                compare=slice(None), sort=True):
+    """Adaptive k refinement of source_grid_adaptive (src/observables/fourier.jl:312-410), level by
+    level: every interval (k1, k3) whose midpoint value (midpoint in ktransform space) is not
+    isapprox the linear interpolation (S1 + S3)/2 at the compared rows is split, and all midpoints of
+    a level are evaluated in one call fun(k_array) -> values[len(k_array), rows, ...].  An interval's
+    decision depends only on its end and midpoint values, so the refined grid is the reference's
+    whatever the evaluation order.  rtol defaults to √eps when atol == 0 (Julia's default)."""
+    f, finv = ktransform
+    rtol = (np.sqrt(np.finfo(float).eps) if atol == 0 else 0.0) if rtol is None else rtol
+    ks = [float(k) for k in ks]
+    if len(ks) < 2:
+        raise ValueError("Initial k-grid must have at least 2 values")
+    for k in (min(ks), max(ks)):
+        if not np.isclose(finv(f(k)), k):
+            raise ValueError("ktransform is not a tuple of inverse functions")
+    vals = list(np.asarray(fun(np.array(ks))))
+    todo = [(i - 1, i) for i in range(1, len(ks))]
+    while todo:
+        if len(ks) + len(todo) > maxks:
+            raise ValueError(f"Source function refinement needs more than {maxks} k-refinements. Reduce refinement criteria.")
+        mids = np.array([finv((f(ks[a]) + f(ks[b])) / 2) for a, b in todo])
+        new = np.asarray(fun(mids))
+        nxt = []
+        for (a, b), km, sm in zip(todo, mids, new):
+            m = len(ks)
+            ks.append(float(km))
+            vals.append(sm)
+            si = (vals[a] + vals[b]) / 2
+            rows = range(sm.shape[0])[compare] if sm.ndim >= 1 else [None]
+            bad = any(not _isapprox(sm[r], si[r], atol, rtol, norm) for r in rows) if sm.ndim >= 1 else \
+                not _isapprox(np.atleast_1d(sm), np.atleast_1d(si), atol, rtol, norm)
+            if bad:
+                nxt += [(m, b), (a, m)]
+        todo = nxt
+    ks = np.array(ks)
+    vals = np.array(vals)
+    if sort:
+        o = np.argsort(ks, kind="stable")
+        ks, vals = ks[o], vals[o]
+    return ks, vals
+
+
+def source_grid_adaptive(prob: CosmologyProblem, taus, ks, *, output="sources", ptivini=-np.inf, cosmo=0, atol=0.0, rtol=None,
+                         norm=np.linalg.norm, ktransform=(lambda k: k, lambda k: k), maxks=1024, sort=True):
+    """source_grid_adaptive (src/observables/fourier.jl:312-410) on the GPU: each refinement level's
+    midpoints are solved in one perturbation launch.  taus = None: final time only.  Returns (ks,
+    values[len(ks), ntau, 3]) for output "sources", (ks, Δm[len(ks)]) for "delta_m"."""
+    prob.solvebg()
+    if taus is None:
+        taus = np.array([prob.bg.tau0[cosmo] * (1 - 1e-12)])
+    taus = np.atleast_1d(np.asarray(taus, dtype=np.float64))
+    nt = len(taus)
+    compare = slice(0, max(nt - 1, 1))  # χ = 0 excluded (sources ∝ 1/χ), unless it is the only time
+
+    def fun(kk):
+        tt = np.broadcast_to(taus, (prob.ncosmo, nt)) if prob.ncosmo > 1 else taus
+        out, st, _ = solvept(prob, kk, ptivini, saveat=None if output == "delta_m" else tt, output=output,
+                             cosmo=np.full(len(kk), cosmo))
+        if np.any(st != 0):
+            raise L.SbzError(f"{int(np.count_nonzero(st))} modes failed during k refinement")
+        return out
+
+    return refine_grid(fun, ks, atol=atol, rtol=rtol, norm=norm, ktransform=ktransform, maxks=maxks, compare=compare, sort=sort)
+
+
 def state_index(M: Model):
     """Map from the oracle/reference ordering [Φ, δc, θc, δb, θb, F0..FLγ, G0..GLγ, N0..NLν, ψ_{j,0..Lh}]
     to this library's state ordering (chains after the photon-baryon head)."""

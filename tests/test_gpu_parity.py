@@ -223,3 +223,22 @@ def test_autotune_picks_a_candidate_and_keeps_results(S):
     got, st, _ = S.solvept(prob, ks, ti, output="delta_m")
     assert np.all(st == 0)
     np.testing.assert_allclose(got, ref, rtol=1e-4)  # another launch shape: same solution to tolerance
+
+
+def test_source_grid_adaptive_on_the_device(S):
+    """source_grid_adaptive (src/observables/fourier.jl:312-410): the refined grid contains the initial
+    one, its values are the solver's at those k, and every split was warranted (each inserted
+    midpoint failed or passed the test against its parents' interpolation as the rule says)."""
+    M = S.ΛCDM(lmax=5)
+    prob = S.CosmologyProblem(M, S.parameters_Planck18(M))
+    ks0 = S.k_from_hMpc(np.geomspace(1e-3, 0.3, 4))
+    bg = prob.solvebg()
+    taus = np.linspace(0.05, bg.tau0[0], 6)
+    ks, vals = S.source_grid_adaptive(prob, taus, ks0, rtol=1e-2, ktransform=(np.log, np.exp), ptivini=1e-6)
+    assert len(ks) > len(ks0) and np.all(np.diff(ks) > 0)
+    assert np.all(np.isin(np.round(ks0, 9), np.round(ks, 9)))
+    direct, st, _ = S.solvept(prob, ks, 1e-6, saveat=taus, output="sources")
+    assert np.all(st == 0)
+    np.testing.assert_allclose(vals, direct, rtol=1e-12, atol=1e-300)
+    kd, dm = S.source_grid_adaptive(prob, None, ks0, output="delta_m", rtol=1e-3, ktransform=(np.log, np.exp), ptivini=1e-6)
+    assert dm.shape == kd.shape and np.all(np.isfinite(dm))

@@ -109,3 +109,45 @@ def test_grids_match_reference_definitions():
     kf = np.linspace(1e-2, 2e3, 1001)
     Mx = ci.matrix(kf)
     np.testing.assert_allclose(Mx @ (ci.xs**2), kf**2, rtol=1e-9)
+
+
+def _reference_refinement(fun, ks, atol, rtol, f, finv):
+    """Direct recursive restatement of the reference's rule (src/observables/fourier.jl:385-394)."""
+    out = {float(k): fun(np.array([k]))[0] for k in ks}
+
+    def split(k1, k3):
+        k2 = float(finv((f(k1) + f(k3)) / 2))
+        s2 = fun(np.array([k2]))[0]
+        out[k2] = s2
+        si = (out[k1] + out[k3]) / 2
+        if any(np.linalg.norm(s2[r] - si[r]) > max(atol, rtol * max(np.linalg.norm(s2[r]), np.linalg.norm(si[r])))
+               for r in range(s2.shape[0])):
+            split(k2, k3)
+            split(k1, k2)
+
+    for a, b in zip(ks[:-1], ks[1:]):
+        split(float(a), float(b))
+    return np.array(sorted(out))
+
+
+def test_adaptive_refinement_matches_the_reference_rule():
+    """Level-synchronous refinement yields the grid of the reference's recursive rule, and every
+    accepted leaf interval passes the midpoint test."""
+    import symboltz as S
+    calls = []
+
+    def fun(kk):
+        calls.append(len(kk))
+        x = np.log(kk)[:, None]
+        return np.concatenate([np.sin(6 * x) * np.exp(-0.1 * x * x), np.cos(3 * x)], axis=1)[:, None, :]  # [k][1 row][2]
+
+    ks0 = np.geomspace(1e-3, 1.0, 5)
+    f, finv = np.log, np.exp
+    got, vals = S.refine_grid(fun, ks0, atol=1e-3, ktransform=(f, finv))
+    ref = _reference_refinement(fun, ks0, 1e-3, 0.0, f, finv)
+    np.testing.assert_allclose(got, ref, rtol=1e-15)
+    assert np.all(np.diff(got) > 0) and set(np.round(ks0, 15)) <= set(np.round(got, 15))
+    assert len(calls) > 2 and max(calls[1:]) > 1  # midpoints are evaluated a level at a time
+    np.testing.assert_allclose(vals[:, 0, :], fun(got)[:, 0, :])
+    with pytest.raises(ValueError):
+        S.refine_grid(fun, ks0, atol=1e-12, ktransform=(f, finv), maxks=64)
