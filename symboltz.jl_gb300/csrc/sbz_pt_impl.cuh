@@ -91,6 +91,8 @@ struct ModeMem {
 template <int NW>
 struct Grp {
   int gt, lane, wq, bar;
+  int fc;          // component of this lane's metric-functional term (n: none; x[n] == 0)
+  unsigned pp;     // bit s: some row of slot s in this warp carries a Φ̇ or Ψ coupling
   mutable int rp;  // ping-pong reduction buffer
   __device__ __forceinline__ void sync() const {
     if constexpr (NW == 1) __syncwarp();
@@ -103,6 +105,22 @@ struct Grp {
 // land on warp 0 as well.
 template <int NW>
 __device__ __forceinline__ int comp_of(int gt, int s) { return s * 32 * NW + ((gt + 32 * s) & (32 * NW - 1)); }
+
+// per-lane model constants kept in registers: the lane's functional component and, per slot,
+// whether any row of this warp carries a Φ̇ or Ψ coupling (warp-uniform; the operator products skip
+// those terms otherwise)
+template <int NW, int NSL>
+__device__ __forceinline__ void init_lane_consts(Grp<NW>& g, const ModelDesc& M, const CompDesc* comps) {
+  const int l = g.lane;
+  g.fc = l < M.npsi ? M.psiComp[l] : (l >= kMaxFun && l - kMaxFun < M.nrho) ? M.rhoComp[l - kMaxFun] : M.n;
+  g.pp = 0;
+#pragma unroll
+  for (int s = 0; s < NSL; ++s) {
+    const int i = comp_of<NW>(g.gt, s);
+    const bool need = i < M.n && (comps[i].phid != CV_ZERO || comps[i].psid != CV_ZERO);
+    if (__any_sync(FULL, need)) g.pp |= 1u << s;
+  }
+}
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -260,12 +278,12 @@ __device__ __forceinline__ void coef_eval(const Grp<NW>& g, ModeMem<NW, NSL, ST>
 
 // Metric functionals of a shared-memory vector v (every warp computes them): Ψ(v) and the δρ
 // sum; Φ̇ = PA·ρ + PB·v_Φ + (-ℋ)Ψ.
+// Lane l < 16 holds the Ψ term of weight w[l], lane 16 + m the δρ term of weight w[16 + m]
+// (kMaxFun = 16); fc is the component it reads (n, a zero entry, when the lane has no term).
 template <typename T>
-__device__ __forceinline__ void functionals(const T* v, const double* w, const ModelDesc& M, double& psi, double& rho) {
+__device__ __forceinline__ void functionals(int fc, const T* v, const double* w, double& psi, double& rho) {
   const int lane = threadIdx.x & 31;
-  double t = 0;
-  if (lane < M.npsi) t = w[lane] * (double)v[M.psiComp[lane]];
-  else if (lane >= kMaxFun && lane - kMaxFun < M.nrho) t = w[lane] * (double)v[M.rhoComp[lane - kMaxFun]];
+  double t = w[lane] * (double)v[fc];
 #pragma unroll
   for (int o = 8; o; o >>= 1) t += __shfl_xor_sync(FULL, t, o);
   psi = __shfl_sync(FULL, t, 0);
@@ -278,12 +296,13 @@ __device__ __forceinline__ double phidot(const double* cv, double rho, double xp
 
 // out = J(τ) x for the thread's components (x in shared memory, complete; x[n] == 0).
 template <int NW, int NSL>
-__device__ __forceinline__ void matvec(int gt, const double* x, const CSet& C, const CompDesc* __restrict__ comps,
+__device__ __forceinline__ void matvec(const Grp<NW>& g, const double* x, const CSet& C, const CompDesc* __restrict__ comps,
                                        const ModelDesc& M, double k, double (&out)[NSL], double* phid_out = nullptr,
                                        double* psi_out = nullptr) {
+  const int gt = g.gt;
   const double* cv = C.cv;
   double psi, rho;
-  functionals(x, C.w, M, psi, rho);
+  functionals(g.fc, x, C.w, psi, rho);
   const double phd = phidot(cv, rho, x[0], psi);
   if (phid_out) *phid_out = phd;
   if (psi_out) *psi_out = psi;
@@ -294,7 +313,8 @@ __device__ __forceinline__ void matvec(int gt, const double* x, const CSet& C, c
     double o = 0;
     if (i < M.n) {
       const CompDesc& D = comps[i];
-      o = cv[D.sp] * (D.A * x[D.ip] + D.C * x[D.inx]) + (cv[D.dg] + cv[D.tr]) * x[i] + cv[D.phid] * phd + cv[D.psid] * psi;
+      o = cv[D.sp] * (D.A * x[D.ip] + D.C * x[D.inx]) + (cv[D.dg] + cv[D.tr]) * x[i];
+      if ((g.pp >> s) & 1u) o += cv[D.phid] * phd + cv[D.psid] * psi;
       if (s == 0 && gt < 32) o += cv[D.e0] * x[D.e0c] + cv[D.e1] * x[D.e1c] + cv[D.e2] * x[D.e2c] + cv[D.dx] * (x[D.dxa] - k34 * x[D.dxb]);
     }
     out[s] = o;
@@ -303,11 +323,12 @@ __device__ __forceinline__ void matvec(int gt, const double* x, const CSet& C, c
 
 // out = (dJ/dτ) x
 template <int NW, int NSL>
-__device__ __forceinline__ void matvec_dtau(int gt, const double* x, const CSet& C, const CompDesc* __restrict__ comps,
+__device__ __forceinline__ void matvec_dtau(const Grp<NW>& g, const double* x, const CSet& C, const CompDesc* __restrict__ comps,
                                             const ModelDesc& M, double k, double (&out)[NSL], double* dpsi_out = nullptr) {
+  const int gt = g.gt;
   double psi, rho, dpsi, drho;
-  functionals(x, C.w, M, psi, rho);
-  functionals(x, C.wd, M, dpsi, drho);
+  functionals(g.fc, x, C.w, psi, rho);
+  functionals(g.fc, x, C.wd, dpsi, drho);
   const double* cv = C.cv; const double* cvd = C.cvd;
   const double phd = phidot(cv, rho, x[0], psi);
   const double dphd = cvd[CV_PA] * rho + cv[CV_PA] * drho + cvd[CV_PB] * x[0] + cvd[CV_MH] * psi + cv[CV_MH] * dpsi;
@@ -319,8 +340,8 @@ __device__ __forceinline__ void matvec_dtau(int gt, const double* x, const CSet&
     double o = 0;
     if (i < M.n) {
       const CompDesc& D = comps[i];
-      o = cvd[D.sp] * (D.A * x[D.ip] + D.C * x[D.inx]) + (cvd[D.dg] + cvd[D.tr]) * x[i] + cvd[D.phid] * phd +
-          cv[D.phid] * dphd + cvd[D.psid] * psi + cv[D.psid] * dpsi;
+      o = cvd[D.sp] * (D.A * x[D.ip] + D.C * x[D.inx]) + (cvd[D.dg] + cvd[D.tr]) * x[i];
+      if ((g.pp >> s) & 1u) o += cvd[D.phid] * phd + cv[D.phid] * dphd + cvd[D.psid] * psi + cv[D.psid] * dpsi;
       if (s == 0 && gt < 32) o += cvd[D.e0] * x[D.e0c] + cvd[D.e1] * x[D.e1c] + cvd[D.e2] * x[D.e2c] + cvd[D.dx] * (x[D.dxa] - k34 * x[D.dxb]);
     }
     out[s] = o;
@@ -492,11 +513,9 @@ __device__ __forceinline__ void solve_M(const Grp<NW>& g, ModeMem<NW, NSL, ST>& 
 
 // Functionals in solve precision from the factorisation's weight copy: Ψ(v), δρ sum, Φ̇.
 template <int NW, int NSL, typename ST>
-__device__ __forceinline__ void functionals_st(const ModeMem<NW, NSL, ST>& W, const ST* v, const ModelDesc& M, ST& psi, ST& phd) {
+__device__ __forceinline__ void functionals_st(const Grp<NW>& g, const ModeMem<NW, NSL, ST>& W, const ST* v, ST& psi, ST& phd) {
   const int lane = threadIdx.x & 31;
-  ST t = 0;
-  if (lane < M.npsi) t = W.wS[lane] * v[M.psiComp[lane]];
-  else if (lane >= kMaxFun && lane - kMaxFun < M.nrho) t = W.wS[lane] * v[M.rhoComp[lane - kMaxFun]];
+  ST t = W.wS[lane] * v[g.fc];
 #pragma unroll
   for (int o = 8; o; o >>= 1) t += __shfl_xor_sync(FULL, t, o);
   psi = __shfl_sync(FULL, t, 0);
@@ -569,8 +588,10 @@ __device__ __forceinline__ void factorize(const Grp<NW>& g, ModeMem<NW, NSL, ST>
   g.sync();
   const int npair = (M.nchain + 1) >> 1;
   if (scan) {
-    // Kogge-Stone multipliers of both chain recurrences, one chain row per lane
-    for (int p = g.wq; p < npair; p += NW) {
+    // Kogge-Stone multipliers of both chain recurrences, one chain row per lane; with several
+    // warps, warp 0 is left to the head inversion below
+    constexpr int w0 = NW > 1 ? 1 : 0, nwp = NW > 1 ? NW - 1 : 1;
+    for (int p = g.wq - w0; p >= 0 && p < npair; p += nwp) {
 #pragma unroll
       for (int hc = 0; hc < 2; ++hc) {
         const int ch = 2 * p + hc;
@@ -652,8 +673,8 @@ __device__ __forceinline__ void factorize(const Grp<NW>& g, ModeMem<NW, NSL, ST>
     if (i < M.n && W.att[i] >= 0) { const ST P = W.bP[i]; W.Z1[i] += P * W.Z1[W.att[i]]; W.Z2[i] += P * W.Z2[W.att[i]]; }
   }
   ST psi1, p1, psi2, p2;
-  functionals_st(W, W.Z1, M, psi1, p1);
-  functionals_st(W, W.Z2, M, psi2, p2);
+  functionals_st(g, W, W.Z1, psi1, p1);
+  functionals_st(g, W, W.Z2, psi2, p2);
   const ST a = 1 - p1, b = -p2, c = -psi1, d = 1 - psi2;
   const ST idet = ST(1) / (a * d - b * c);
   F.S00 = d * idet; F.S01 = -b * idet; F.S10 = -c * idet; F.S11 = a * idet;
@@ -666,7 +687,7 @@ __device__ __forceinline__ void solve_W(const Grp<NW>& g, ModeMem<NW, NSL, ST>& 
                                         bool scan) {
   solve_M<1>(g, W, M, F, scan, W.r, W.r);
   ST psi, ph;
-  functionals_st(W, W.r, M, psi, ph);
+  functionals_st(g, W, W.r, psi, ph);
   const ST t0 = F.S00 * ph + F.S01 * psi, t1 = F.S10 * ph + F.S11 * psi;
 #pragma unroll
   for (int sl = 0; sl < NSL; ++sl) {
@@ -702,7 +723,7 @@ __device__ __forceinline__ void stage_solve(const Grp<NW>& g, ModeMem<NW, NSL, S
     for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) W.x[i] = U[sl]; }
     g.sync();
     double JU[NSL];
-    matvec<NW, NSL>(gt, W.x, CJ, comps, M, k, JU);
+    matvec<NW, NSL>(g, W.x, CJ, comps, M, k, JU);
 #pragma unroll
     for (int sl = 0; sl < NSL; ++sl) {
       const int i = comp_of<NW>(gt, sl);
@@ -747,12 +768,12 @@ __device__ void emit_output(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const PtA
   for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) W.x[i] = y[sl]; }
   g.sync();
   double fy[NSL], dJy[NSL], Jf[NSL], phid, psi, dpsi_w, psi_f;
-  matvec<NW, NSL>(gt, W.x, CS, comps, M, k, fy, &phid, &psi);
-  matvec_dtau<NW, NSL>(gt, W.x, CS, comps, M, k, dJy, &dpsi_w);
+  matvec<NW, NSL>(g, W.x, CS, comps, M, k, fy, &phid, &psi);
+  matvec_dtau<NW, NSL>(g, W.x, CS, comps, M, k, dJy, &dpsi_w);
 #pragma unroll
   for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) W.f[i] = fy[sl]; }
   g.sync();
-  matvec<NW, NSL>(gt, W.f, CS, comps, M, k, Jf, nullptr, &psi_f);
+  matvec<NW, NSL>(g, W.f, CS, comps, M, k, Jf, nullptr, &psi_f);
   if (g.wq == 0) {
     // second derivative of Π = F2 + G0 + G2 along the flow: (J'y + J f) restricted to those rows
     double gv = 0;
@@ -887,7 +908,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
       g.sync();
       // Φ from k²(Φ - Ψ) = 12πa²Π with the initial shears: Ψ(y) is linear with unit weight on Φ
       double psi0, rho0;
-      functionals(W.x, W.cs[sIC].w, M, psi0, rho0);  // Φ slot still 0
+      functionals(g.fc, W.x, W.cs[sIC].w, psi0, rho0);  // Φ slot still 0
       g.sync();
       if (gt == 0) { y[0] = Psi - psi0; W.x[0] = y[0]; }
       g.sync();
@@ -917,7 +938,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
 #pragma unroll
       for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl]; }
       g.sync();
-      matvec<NW, NSL>(gt, W.x, W.cs[sJ], comps, M, k, f0);
+      matvec<NW, NSL>(g, W.x, W.cs[sJ], comps, M, k, f0);
       // initial step (Hairer-Nørsett-Wanner II.4)
       double h;
       {
@@ -935,7 +956,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         const double th = t + h0;
         coef_eval(g, W, &s5, &th, 1, 0u, false, cd, tab, M.nexpr, M.nx, mk);
         double f1[NSL];
-        matvec<NW, NSL>(gt, W.x, W.cs[s5], comps, M, k, f1);
+        matvec<NW, NSL>(g, W.x, W.cs[s5], comps, M, k, f1);
         double d2 = 0;
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) {
@@ -964,7 +985,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
 #pragma unroll
           for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl]; }
           g.sync();
-          matvec_dtau<NW, NSL>(gt, W.x, CJ, comps, M, k, ft);
+          matvec_dtau<NW, NSL>(g, W.x, CJ, comps, M, k, ft);
           have_jac = true;
         }
         const double ih = 1.0 / h, s = 4.0 * ih;  // s = 1/(hγ), γ = 1/4
@@ -993,7 +1014,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl] + rw::A21 * U1[sl]; }
         g.sync();
-        matvec<NW, NSL>(gt, W.x, W.cs[s2], comps, M, k, Fv);
+        matvec<NW, NSL>(g, W.x, W.cs[s2], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C21 * U1[sl]) + h * rw::d2 * ft[sl];
         stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U2);
@@ -1001,7 +1022,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl] + rw::A31 * U1[sl] + rw::A32 * U2[sl]; }
         g.sync();
-        matvec<NW, NSL>(gt, W.x, W.cs[s3], comps, M, k, Fv);
+        matvec<NW, NSL>(g, W.x, W.cs[s3], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C31 * U1[sl] + rw::C32 * U2[sl]) + h * rw::d3 * ft[sl];
         stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U3);
@@ -1009,7 +1030,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl] + rw::A41 * U1[sl] + rw::A42 * U2[sl] + rw::A43 * U3[sl]; }
         g.sync();
-        matvec<NW, NSL>(gt, W.x, W.cs[s4], comps, M, k, Fv);
+        matvec<NW, NSL>(g, W.x, W.cs[s4], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C41 * U1[sl] + rw::C42 * U2[sl] + rw::C43 * U3[sl]) + h * rw::d4 * ft[sl];
         stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U4);
@@ -1022,7 +1043,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
           if (i < n) W.x[i] = Y[sl];
         }
         g.sync();
-        matvec<NW, NSL>(gt, W.x, W.cs[s5], comps, M, k, Fv);
+        matvec<NW, NSL>(g, W.x, W.cs[s5], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C51 * U1[sl] + rw::C52 * U2[sl] + rw::C53 * U3[sl] + rw::C54 * U4[sl]);
         stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U5);
@@ -1030,7 +1051,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); Y[sl] += U5[sl]; if (i < n) W.x[i] = Y[sl]; }
         g.sync();
-        matvec<NW, NSL>(gt, W.x, W.cs[s5], comps, M, k, Fv);
+        matvec<NW, NSL>(g, W.x, W.cs[s5], comps, M, k, Fv);
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C61 * U1[sl] + rw::C62 * U2[sl] + rw::C63 * U3[sl] + rw::C64 * U4[sl] + rw::C65 * U5[sl]);
         stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U6);
@@ -1065,7 +1086,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
           for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y1[sl]; }
           g.sync();
           double f1[NSL];
-          matvec<NW, NSL>(gt, W.x, W.cs[s5], comps, M, k, f1);
+          matvec<NW, NSL>(g, W.x, W.cs[s5], comps, M, k, f1);
           // the t1 coefficient set becomes the next step's Jacobian set
           { const int tsw = sJ; sJ = s5; s5 = tsw; }
           if (taus) {
@@ -1183,6 +1204,7 @@ __global__ void __launch_bounds__(128) pt_kernel(PtArgs A) {
   g.wq = g.gt >> 5;
   g.bar = 1 + grp;
   g.rp = 0;
+  init_lane_consts<NW, NSL>(g, M, comps);
   pt_body<NW, NSL, ST>(A, M, comps, Wm[grp], g);
 }
 
@@ -1221,6 +1243,7 @@ __global__ void __launch_bounds__(32) rhs_kernel(PtArgs A, const double* __restr
   for (int i = g.gt; i < (int)sizeof(ModelDesc) / 4; i += 32) reinterpret_cast<int*>(&M)[i] = reinterpret_cast<const int*>(A.model)[i];
   for (int i = g.gt; i < A.model_n * (int)sizeof(CompDesc) / 4; i += 32) reinterpret_cast<int*>(comps)[i] = reinterpret_cast<const int*>(A.comps)[i];
   __syncwarp();
+  init_lane_consts<1, NSL>(g, M, comps);
   const int n = M.n, item = blockIdx.x;
   for (int i = g.gt; i < kNSets * (int)(sizeof(CSet) / sizeof(double)); i += 32) reinterpret_cast<double*>(W.cs)[i] = 0;
   for (int i = n + g.gt; i <= 32 * NSL; i += 32) W.x[i] = 0;
@@ -1236,8 +1259,8 @@ __global__ void __launch_bounds__(32) rhs_kernel(PtArgs A, const double* __restr
   for (int i = g.gt; i < n; i += 32) W.x[i] = y_in[(size_t)item * n + i];
   __syncwarp();
   double f[NSL], ft[NSL];
-  matvec<1, NSL>(g.gt, W.x, W.cs[0], comps, M, mk.k, f);
-  matvec_dtau<1, NSL>(g.gt, W.x, W.cs[0], comps, M, mk.k, ft);
+  matvec<1, NSL>(g, W.x, W.cs[0], comps, M, mk.k, f);
+  matvec_dtau<1, NSL>(g, W.x, W.cs[0], comps, M, mk.k, ft);
 #pragma unroll
   for (int sl = 0; sl < NSL; ++sl) {
     const int i = g.gt + 32 * sl;
