@@ -136,12 +136,8 @@ def run_ours(args):
     import symboltz as S
 
     assert torch.cuda.is_available(), "bench needs a GPU"
-    rank = int(os.environ.get("RANK", 0))
-    world = int(os.environ.get("WORLD_SIZE", 1))
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    from symboltz import replicas as R
+    rank, world = R.init("nccl")  # replicas: each rank runs the whole workload, no data-path collective
     M = S.ΛCDM(lmax_gamma=MODEL["lmax_gamma"], lmax_nu=MODEL["lmax_nu"], lmax_h=MODEL["lmax_h"], nx=MODEL["nx"])
     prob = S.CosmologyProblem(M, PARAMS, precision=args.precision, refine_skip=REFINE_SKIP_CL)
     ks, taus, ls = workload_grids(S, prob)
@@ -166,8 +162,7 @@ def run_ours(args):
         for _ in range(args.steps):
             flush.fill_(1.0)
             torch.cuda.synchronize()
-            if world > 1:
-                torch.distributed.barrier()
+            R.barrier()
             e0.record(stream)
             Dl, st = step()
             e1.record(stream)
@@ -197,10 +192,7 @@ def run_ours(args):
     steps_total = int(stp.sum())
     dev = float(np.sum(dev_ms))
     e2e = float(np.sum(e2e_ms))
-    if world > 1:
-        tt = torch.tensor([dev, e2e], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        dev, e2e = tt.tolist()
+    dev, e2e = R.reduce_over_ranks([dev, e2e], op="max")
     K = args.steps
     tau0 = float(prob.solvebg().tau0[0])
     nk_fine = int(len(S.lingrid(float(ks.min()), float(ks.max()), step=np.pi / tau0)))
@@ -237,8 +229,7 @@ def run_ours(args):
         line["cpu_baseline"] = cpu_baseline(seconds=args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    R.finalize()
 
 
 def cpu_baseline(seconds=20.0, impl_line=False):

@@ -92,6 +92,11 @@ int sbz_momentum_quadrature(int N, double* x, double* W);
 int sbz_problem_create(const sbz_model* m, const sbz_params* p, int n_cosmo, const sbz_opts* o, sbz_problem** out);
 void sbz_problem_destroy(sbz_problem* pb);
 int sbz_problem_nstate(const sbz_problem* pb);
+/* Replace the parameter sets of an existing problem (batched parameter upload; the problem-level
+ * form of parameter_updater, src/solve.jl:271-306).  The model, options, stream and device buffers
+ * are kept (buffers grow when n_cosmo does); the background must be solved again before the next
+ * perturbation call.  Waits for the problem's stream first. */
+int sbz_problem_set_params(sbz_problem* pb, const sbz_params* p, int n_cosmo);
 
 /* solvebg (src/solve.jl:427-435) with the a = 1 callback (src/solve.jl:158-203): τ0, κ0, τrec and
  * status per cosmology (arrays of n_cosmo, any may be NULL).  Also builds and uploads the

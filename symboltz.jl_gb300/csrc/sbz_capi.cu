@@ -173,6 +173,17 @@ int sbz_problem_create(const sbz_model* m, const sbz_params* p, int n_cosmo, con
   return SBZ_OK;
 }
 
+int sbz_problem_set_params(sbz_problem* pb, const sbz_params* p, int n_cosmo) {
+  if (!pb || !p || n_cosmo < 1) return fail(SBZ_ERR_ARG, "sbz_problem_set_params: bad arguments");
+  if (pb->stream && cudaStreamSynchronize(pb->stream) != cudaSuccess) return fail(SBZ_ERR_CUDA, "stream");
+  pb->params.assign(p, p + n_cosmo);
+  pb->ncosmo = n_cosmo;
+  pb->bgs.clear(); pb->bg_status.clear(); pb->cds.clear();
+  pb->bg_done = false;
+  pb->tables_uploaded = false;
+  return SBZ_OK;
+}
+
 // Device resources are created on first use, so the host stages (background, tables) run
 // without a GPU.
 static int ensure_device(sbz_problem* pb) {

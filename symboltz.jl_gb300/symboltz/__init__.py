@@ -23,7 +23,7 @@ __all__ = [
     "ΛCDM", "LCDM", "parameters_Planck18", "CosmologyProblem", "CosmologySolution", "solve", "solvebg", "solvept",
     "issuccess", "spectrum_primordial", "spectrum_matter", "source_grid", "SphericalBesselCache", "los_integrate",
     "spectrum_cmb", "lingrid", "loggrid", "cosgrid", "ChebyshevInterpolator", "CubicSplineInterpolator",
-    "momentum_quadrature", "k_from_hMpc", "SbzError",
+    "momentum_quadrature", "k_from_hMpc", "SbzError", "parameter_updater", "source_grid_adaptive",
 ]
 
 C_LIGHT = 299792458.0
@@ -130,6 +130,16 @@ class CosmologyProblem:
             L.lib().sbz_problem_destroy(h)
             self._h = None
 
+    def set_params(self, pars):
+        """Replace the parameter sets in place (one dict or a list; the count may change), keeping the
+        model, options, stream and device buffers; the background is solved again on next use."""
+        self.pars = [dict(p) for p in ([pars] if isinstance(pars, dict) else pars)]
+        pc, n = _params_c(self.pars)
+        L.check(L.lib().sbz_problem_set_params(self._h, pc, n), "set_params")
+        self.ncosmo = n
+        self.bg = None
+        return self
+
     def solvebg(self):
         if self.bg is None:
             n = self.ncosmo
@@ -170,6 +180,37 @@ class BackgroundSolution:
         out = np.zeros((len(taus), 7))
         L.check(L.lib().sbz_bg_coefficients(self.prob._h, c, len(taus), L.dptr(taus), L.dptr(out)), "bg_coefficients")
         return out
+
+
+def parameter_updater(prob: CosmologyProblem, idxs, *, inplace=False):
+    """parameter_updater(prob, idxs) (src/solve.jl:271-306): a function that takes values for the
+    parameter names `idxs` (a sequence in that order, or a dict by name) and returns a problem with
+    them updated.  Like the reference it returns a new problem and leaves `prob` as it was; with
+    inplace=True it re-uploads into `prob` itself (sbz_problem_set_params: no new device
+    allocations).  A 2-D array of values (one row per cosmology) updates that many parameter sets,
+    the unnamed parameters taken from the first of `prob`'s."""
+    idxs = list(idxs)
+    for k in idxs:
+        if k not in _PKEYS:
+            raise KeyError(f"unknown parameter {k!r}; known: {', '.join(_PKEYS)}")
+
+    def updater(p):
+        rows = [[p[k] for k in idxs]] if isinstance(p, dict) else np.atleast_2d(np.asarray(p, dtype=np.float64))
+        if np.shape(rows)[1] != len(idxs):
+            raise ValueError(f"expected {len(idxs)} values per parameter set")
+        new = [dict(prob.pars[0], **{k: float(v) for k, v in zip(idxs, row)}) for row in rows]
+        if inplace:
+            return prob.set_params(new)
+        o = prob.opts
+        return CosmologyProblem(prob.M, new, bg_rtol=o.bg_rtol, bg_atol=o.bg_atol, pt_rtol=o.pt_rtol, pt_atol=o.pt_atol,
+                                ivspan=(o.tau_ini, o.tau_max), maxiters=o.maxiters,
+                                precision={L.SBZ_MIXED: "mixed", L.SBZ_FP64: "fp64"}[o.precision], refine_iters=o.refine_iters,
+                                table_points=o.table_points, warps_per_block=o.warps_per_block, warps_per_mode=o.warps_per_mode,
+                                blocks_per_sm=o.blocks_per_sm,
+                                los_precision=None if o.los_precision < 0 else {L.SBZ_FP64: "fp64", L.SBZ_MIXED: "mixed"}[o.los_precision],
+                                refine_skip=o.refine_skip)
+
+    return updater
 
 
 def solvebg(prob: CosmologyProblem):
@@ -369,8 +410,20 @@ def spectrum_primordial(k, prob: CosmologyProblem, c=0):
     return P0
 
 
-def spectrum_matter(prob: CosmologyProblem, ks, *, kτini=1e-2, τinimax=1e-4, cosmo=None, return_status=False):
-    """Linear P(k, τ0) = P0 Δ_m² (src/observables/fourier.jl:79-101)."""
+def spectrum_matter(prob: CosmologyProblem, ks, *, kτini=1e-2, τinimax=1e-4, cosmo=None, return_status=False,
+                    sourceopts=None, coarse_length=9):
+    """Linear P(k, τ0) = P0 Δ_m² (src/observables/fourier.jl:79-101).
+
+    ks = (kmin, kmax): the adaptive form (fourier.jl:103-125) — a coarse_length-point log grid
+    refined in log k until Δ_m at each midpoint is within sourceopts (default atol 4, rtol 4e-3) of
+    the linear interpolation, modes started at the first background time; returns (ks, P)."""
+    if isinstance(ks, tuple) and len(ks) == 2:
+        c = 0 if cosmo is None else int(cosmo)
+        kmin, kmax = (float(k) for k in ks)
+        k0 = loggrid(kmin, kmax, length=coarse_length)
+        opts = dict(atol=4.0, rtol=4e-3) if sourceopts is None else dict(sourceopts)
+        kk, dm = source_grid_adaptive(prob, None, k0, output="delta_m", cosmo=c, ktransform=(np.log, np.exp), **opts)
+        return kk, spectrum_primordial(kk, prob, c) * dm**2
     prob.solvebg()
     ks = L.f64(np.atleast_1d(ks))
     nk = len(ks)

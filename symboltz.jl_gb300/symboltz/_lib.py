@@ -17,7 +17,7 @@ SBZ_FP64, SBZ_MIXED = 0, 1
 SBZ_OUT_SOURCES, SBZ_OUT_DELTA_M, SBZ_OUT_STATE, SBZ_OUT_SOURCES4, SBZ_OUT_FACTORS = 0, 1, 2, 3, 4
 
 EXPORTS = (
-    "sbz_default_opts", "sbz_last_error", "sbz_momentum_quadrature", "sbz_problem_create", "sbz_problem_destroy",
+    "sbz_default_opts", "sbz_last_error", "sbz_momentum_quadrature", "sbz_problem_create", "sbz_problem_destroy", "sbz_problem_set_params",
     "sbz_problem_nstate", "sbz_solve_bg", "sbz_bg_knots", "sbz_bg_eval", "sbz_bg_coefficients", "sbz_solve_pt", "sbz_solve_pt_device", "sbz_pt_rhs",
     "sbz_spectrum_matter", "sbz_spectrum_primordial", "sbz_bessel_create", "sbz_bessel_destroy", "sbz_bessel_eval",
     "sbz_los_integrate", "sbz_los_integrate_device", "sbz_cl_integrate", "sbz_cl_integrate_noalloc", "sbz_autotune_pt", "sbz_mlp_gemm", "sbz_surrogate_create", "sbz_surrogate_destroy", "sbz_surrogate_nparams",
@@ -66,6 +66,7 @@ def lib():
     L.sbz_last_error.restype = C.c_char_p
     L.sbz_momentum_quadrature.argtypes = [C.c_int, dp, dp]
     L.sbz_problem_create.argtypes = [C.POINTER(Model), C.POINTER(Params), C.c_int, C.POINTER(Opts), C.POINTER(vp)]
+    L.sbz_problem_set_params.argtypes = [vp, C.POINTER(Params), C.c_int]
     L.sbz_problem_destroy.argtypes = [vp]
     L.sbz_problem_destroy.restype = None
     L.sbz_problem_nstate.argtypes = [vp]

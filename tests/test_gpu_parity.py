@@ -244,3 +244,50 @@ def test_source_grid_adaptive_on_the_device(S):
     np.testing.assert_allclose(vals, direct, rtol=1e-12, atol=1e-300)
     kd, dm = S.source_grid_adaptive(prob, None, ks0, output="delta_m", rtol=1e-3, ktransform=(np.log, np.exp), ptivini=1e-6)
     assert dm.shape == kd.shape and np.all(np.isfinite(dm))
+
+
+def test_adaptive_spectrum_matter(S, bg5):
+    """spectrum_matter(prob, (kmin, kmax)) (src/observables/fourier.jl:103-125): 9-point log grid
+    refined on Δ_m (atol 4, rtol 4e-3).  The refined grid is the oracle's (same rule driven by the
+    oracle's Δ_m), the values are the solver's at those k, and P(k) matches the oracle there."""
+    M = S.ΛCDM(lmax=5)
+    prob = S.CosmologyProblem(M, S.parameters_Planck18(M))
+    kmin, kmax = S.k_from_hMpc(1e-4), S.k_from_hMpc(1.0)
+    ks, P = S.spectrum_matter(prob, (kmin, kmax))
+    assert ks[0] == kmin and ks[-1] == kmax and len(ks) > 9 and np.all(np.diff(ks) > 0)
+    dm, st, _ = S.solvept(prob, ks, -np.inf, output="delta_m")
+    assert np.all(st == 0)
+    np.testing.assert_allclose(P, S.spectrum_primordial(ks, prob) * dm**2, rtol=1e-12)
+
+    def oracle_dm(kk):
+        out, sto, _ = bg5.solve_pt(kk, bg5.t[0], None, mode=1)
+        assert np.all(sto == 0)
+        return out
+    ko, dmo = S.refine_grid(oracle_dm, S.loggrid(kmin, kmax, length=9), atol=4.0, rtol=4e-3, ktransform=(np.log, np.exp))
+    assert len(ko) == len(ks)
+    np.testing.assert_allclose(ks, ko, rtol=1e-14)
+    assert np.linalg.norm(dm - dmo) <= 1e-4 * np.linalg.norm(dmo)  # the P(k) parity bar, normwise
+
+
+def test_set_params_reuses_the_problem(S):
+    """sbz_problem_set_params: the same handle, re-uploaded with 1 then 3 parameter sets, gives
+    bit-identical modes to fresh problems (stale device tables would show here)."""
+    M = S.ΛCDM(lmax=5)
+    base = S.parameters_Planck18(M)
+    ks = S.k_from_hMpc(S.loggrid(1e-4, 1.0, length=24))
+    ti = lambda k: np.minimum(1e-2 / k, 1e-4)  # noqa: E731
+    p = S.CosmologyProblem(M, base, warps_per_mode=2)
+    S.solvept(p, ks, ti, output="delta_m")
+    sets = [dict(base, h=0.7), dict(base, h=0.64, Omega_b=0.05), dict(base, ns=0.95), dict(base, h=0.71, Omega_c=0.3)]
+    p.set_params(sets[0])
+    got, st, _ = S.solvept(p, ks, ti, output="delta_m")
+    ref, _, _ = S.solvept(S.CosmologyProblem(M, sets[0], warps_per_mode=2), ks, ti, output="delta_m")
+    assert np.all(st == 0)
+    np.testing.assert_array_equal(got, ref)
+    p.set_params(sets[1:])
+    cos = np.repeat(np.arange(3), len(ks))
+    got, st, _ = S.solvept(p, np.tile(ks, 3), ti, output="delta_m", cosmo=cos)
+    assert np.all(st == 0)
+    for i in range(3):
+        one, _, _ = S.solvept(S.CosmologyProblem(M, sets[1 + i], warps_per_mode=2), ks, ti, output="delta_m")
+        np.testing.assert_array_equal(got[cos == i], one)

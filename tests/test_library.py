@@ -70,6 +70,37 @@ def test_host_stages_run_and_gpu_calls_fail_loudly_without_gpu():
         S.spectrum_matter(p, [1.0])
 
 
+def test_parameter_updates_equal_fresh_problems():
+    """parameter_updater (src/solve.jl:271-306): a new problem by default, the same handle with
+    inplace=True, several parameter sets from a 2-D array; backgrounds equal fresh problems'."""
+    from symboltz import _lib
+    import symboltz as S
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("library not built")
+    M = S.ΛCDM(lmax=5)
+    base = S.parameters_Planck18()
+    p = S.CosmologyProblem(M, base)
+    tau0 = p.solvebg().tau0[0]
+    upd = S.parameter_updater(p, ["h", "Omega_c"])
+    q = upd([0.7, 0.25])
+    assert q is not p and p.pars[0]["h"] == base["h"] and p.solvebg().tau0[0] == tau0
+    fresh = S.CosmologyProblem(M, dict(base, h=0.7, Omega_c=0.25))
+    assert q.solvebg().tau0[0] == fresh.solvebg().tau0[0] != tau0
+    assert q.opts.pt_rtol == p.opts.pt_rtol and q.opts.precision == p.opts.precision
+    same = S.parameter_updater(p, ["h", "Omega_c"], inplace=True)({"h": 0.7, "Omega_c": 0.25})
+    assert same is p and p.bg is None and p.solvebg().tau0[0] == fresh.solvebg().tau0[0]
+    rows = np.array([[0.65, 0.3], [0.72, 0.22], [0.68, 0.27]])
+    S.parameter_updater(p, ["h", "Omega_c"], inplace=True)(rows)
+    bg = p.solvebg()
+    assert p.ncosmo == 3 and len(bg.tau0) == 3
+    for i, (h, oc) in enumerate(rows):
+        assert bg.tau0[i] == S.CosmologyProblem(M, dict(base, h=h, Omega_c=oc)).solvebg().tau0[0]
+    with pytest.raises(KeyError):
+        S.parameter_updater(p, ["H0"])
+    with pytest.raises(ValueError):
+        S.parameter_updater(p, ["h"])([0.7, 0.2])
+
+
 def test_background_and_table_match_oracle():
     """The product's host background (solve, spline, coefficient table) against the oracle."""
     from symboltz import _lib
