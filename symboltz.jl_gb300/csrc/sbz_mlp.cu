@@ -53,12 +53,16 @@ int launch(const GemmArgs& g, const void* A, const void* B, cudaStream_t st) {
   if (!tmap_rows_k(&ta, A, g.M, g.K, BM) || !tmap_rows_k(&tb, B, g.N, g.K, BN)) return SBZ_ERR_CUDA;
   const size_t smem = gemm_smem_bytes<BN>();
   auto k = gemm_tn_kernel<BN>;
-  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return SBZ_ERR_CUDA;
+  static bool attr_set = false;  // set once, outside any stream capture of a later call
+  if (!attr_set) {
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return SBZ_ERR_CUDA;
+    attr_set = true;
+  }
   const int tiles = (g.N / BN) * (g.M / BM), KT = g.K / BK;
-  // weight gradients have few output tiles and a long K (the batch): split K over ~2 CTAs per SM,
-  // at least 4 K-steps each, and add the partial tiles atomically into a zeroed output
+  // weight gradients have few output tiles and a long K (the batch): split K over about one CTA
+  // per SM, at least 4 K-steps each, and add the partial tiles atomically into a zeroed output
   int splits = 1;
-  if (g.epi == EPI_F32 && tiles < num_sms()) splits = std::max(1, std::min(KT / 4, (2 * num_sms() + tiles - 1) / tiles));
+  if (g.epi == EPI_F32 && tiles < num_sms()) splits = std::max(1, std::min(KT / 4, num_sms() / tiles));
   if (splits > 1 && !g.accumulate) {
     for (int r = 0; r < g.M; ++r) {  // rows of the output region (ldo may exceed N)
       if (g.ldo == g.n_valid) {
@@ -69,7 +73,7 @@ int launch(const GemmArgs& g, const void* A, const void* B, cudaStream_t st) {
     }
   }
   const dim3 grid(g.N / BN, g.M / BM, splits);
-  k<<<grid, 128, smem, st>>>(ta, tb, g);
+  k<<<grid, kThreads, smem, st>>>(ta, tb, g);
   return cudaGetLastError() == cudaSuccess ? SBZ_OK : SBZ_ERR_CUDA;
 }
 

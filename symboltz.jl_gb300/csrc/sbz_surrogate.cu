@@ -4,13 +4,18 @@
 // Layout: layer l maps kin_l → nrow_l features; the input is padded to 64 columns and the output
 // to 64 rows (TMA/UMMA granularity), padding weights stay zero (their gradients are zero).  Master
 // weights, Adam moments and gradients are FP32 [nrow][kin]; the GEMMs read BF16 copies W [nrow][kin]
-// (forward) and Wt [kin][nrow] (backward).  Activations are BF16 [batch][features]; the last layer
-// writes FP32 so the loss is not quantised.  A training step:
-//   forward   X_l = SiLU(X_{l-1} W_lᵀ + b_l)          (EPI_ACT, pre-activations Z_l kept)
-//   loss      Y = X_L W_Lᵀ + b_L (FP32), dY = 2 (Y - T) / (batch · nout)
-//   backward  dZ_{l-1} = (dZ_l W_l) ⊙ SiLU'(Z_{l-1})  (EPI_DACT)
-//             dW_l = dZ_lᵀ X_{l-1} (EPI_F32 on transposed operands), db_l = Σ_batch dZ_l
-//   Adam      FP32 update, then BF16 W and Wt refreshed.
+// (forward) and Wt [kin][nrow] (backward).  Activations are BF16 [batch][features], each with a
+// transposed copy [features][batch] written by the same epilogue (the weight-gradient GEMMs read
+// the batch as their K dimension); the last layer writes FP32 so the loss is not quantised.  A
+// training step:
+//   gather    X_0 (and X_0ᵀ), targets T of the step's random batch
+//   forward   X_l = SiLU(X_{l-1} W_lᵀ + b_l)          (EPI_ACT, pre-activations Z_l kept, X_lᵀ)
+//   loss      Y = X_L W_Lᵀ + b_L (FP32), dY = 2 (Y - T) / (batch · nout), dYᵀ, db_L = Σ_batch dY
+//   backward  dZ_{l-1} = (dZ_l W_l) ⊙ SiLU'(Z_{l-1})  (EPI_DACT, dZ_{l-1}ᵀ and db_{l-1} = Σ_batch dZ_{l-1})
+//             dW_l = dZ_lᵀ X_{l-1} (EPI_F32 on the transposed copies, split K)
+//   Adam      one launch over every parameter: FP32 update, BF16 W and Wt refreshed.
+// The step (about 20 launches) is captured once in a CUDA graph and replayed; the step counter
+// and the learning rate live in device memory so the replayed graph needs no new parameters.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <cmath>
@@ -62,6 +67,13 @@ struct sbz_surrogate {
   long long step = 0;
   unsigned long long seed = 0;
   cudaStream_t stream = nullptr;
+  long long* dstep = nullptr;  // device step counter (incremented at the start of each step)
+  float* dlr = nullptr;        // device learning rate
+  void* segs = nullptr;        // device table of Adam segments
+  int nseg = 0;
+  long long nparam_all = 0;    // padded parameter count over all segments
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
 };
 
 namespace {
@@ -76,39 +88,65 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
   return z ^ (z >> 31);
 }
 
+// dstep (if not null) replaces step: the graph-captured training step reads the device counter.
+// X0t (if not null) receives the transposed copy [kPadIn][batch].
 __global__ void gather_batch(int batch, int nin, int nout, const float* __restrict__ dX, const float* __restrict__ dY, long long n,
-                             long long step, unsigned long long seed, long long offset, int random, bf16* __restrict__ X0,
-                             float* __restrict__ T) {
+                             long long step, const long long* __restrict__ dstep, unsigned long long seed, long long offset, int random,
+                             bf16* __restrict__ X0, bf16* __restrict__ X0t, float* __restrict__ T) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= batch) return;
+  if (dstep) step = *dstep;
   long long r;
   if (random) r = (long long)(mix64(seed ^ mix64((unsigned long long)step * 0x100000001B3ull + (unsigned long long)i)) % (unsigned long long)n);
   else r = offset + i;
   const bool live = r < n;
   bf16* x = X0 + (size_t)i * kPadIn;
-  for (int j = 0; j < kPadIn; ++j) x[j] = __float2bfloat16(live && j < nin ? dX[(size_t)r * nin + j] : 0.0f);
+  for (int j = 0; j < kPadIn; ++j) {
+    const bf16 v = __float2bfloat16(live && j < nin ? dX[(size_t)r * nin + j] : 0.0f);
+    x[j] = v;
+    if (X0t) X0t[(size_t)j * batch + i] = v;
+  }
   if (T)
     for (int j = 0; j < nout; ++j) T[(size_t)i * nout + j] = live ? dY[(size_t)r * nout + j] : 0.0f;
 }
 
-// loss and output gradient: y = Yf + b (FP32), r = y - t, dY = 2 r / (batch · nout) (BF16, padding 0)
-__global__ void loss_grad(int batch, int nout, const float* __restrict__ Yf, const float* __restrict__ b, const float* __restrict__ T,
-                          bf16* __restrict__ dY, double* __restrict__ loss) {
+__global__ void begin_step(long long* step, double* loss) {
+  ++*step;
+  *loss = 0.0;
+}
+
+__global__ void set_value(float* dst, float v) { *dst = v; }
+
+// loss and output gradient: y = Yf + b (FP32), r = y - t, dY = 2 r / (batch · nout) (BF16, padding 0);
+// also dYᵀ [kPadOut][batch] and the bias gradient gb[j] += Σ_rows dY[.][j] (as rounded), when not null.
+// 256 threads per block.
+constexpr int kLossThreads = 256;
+__global__ void __launch_bounds__(kLossThreads) loss_grad(int batch, int nout, const float* __restrict__ Yf, const float* __restrict__ b,
+                                                           const float* __restrict__ T, bf16* __restrict__ dY, bf16* __restrict__ dYt,
+                                                           float* __restrict__ gb, double* __restrict__ loss) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ float cs[kLossThreads / 32][kPadOut];
   double l = 0;
-  if (i < batch) {
-    const float sc = 2.0f / ((float)batch * nout);
-    for (int j = 0; j < kPadOut; ++j) {
-      float g = 0.0f;
-      if (j < nout) {
-        const float r = Yf[(size_t)i * kPadOut + j] + b[j] - T[(size_t)i * nout + j];
-        l += (double)r * r;
-        g = sc * r;
-      }
-      dY[(size_t)i * kPadOut + j] = __float2bfloat16(g);
+  const float sc = 2.0f / ((float)batch * nout);
+  for (int j = 0; j < kPadOut; ++j) {
+    float g = 0.0f;
+    if (i < batch && j < nout) {
+      const float r = Yf[(size_t)i * kPadOut + j] + b[j] - T[(size_t)i * nout + j];
+      l += (double)r * r;
+      g = sc * r;
+    }
+    const bf16 gh = __float2bfloat16(g);
+    if (i < batch) {
+      dY[(size_t)i * kPadOut + j] = gh;
+      if (dYt) dYt[(size_t)j * batch + i] = gh;
+    }
+    if (gb && j < nout) {
+      float w = __bfloat162float(gh);
+      for (int o = 16; o; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+      if ((threadIdx.x & 31) == 0) cs[threadIdx.x >> 5][j] = w;
     }
   }
-  __shared__ double red[8];
+  __shared__ double red[kLossThreads / 32];
   for (int o = 16; o; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = l;
   __syncthreads();
@@ -117,37 +155,42 @@ __global__ void loss_grad(int batch, int nout, const float* __restrict__ Yf, con
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
     atomicAdd(loss, s / ((double)batch * nout));
   }
-}
-
-// out[c][r] = in[r][c] for an R x C bf16 matrix (R, C multiples of 32); colsum[c] += Σ_r in[r][c]
-__global__ void transpose_bf16(int R, int C, const bf16* __restrict__ in, bf16* __restrict__ out, float* __restrict__ colsum) {
-  __shared__ float tile[32][33];
-  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
-  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
-  for (int k = ty; k < 32; k += 8) tile[k][tx] = __bfloat162float(in[(size_t)(r0 + k) * C + c0 + tx]);
-  __syncthreads();
-  for (int k = ty; k < 32; k += 8) out[(size_t)(c0 + k) * R + r0 + tx] = __float2bfloat16(tile[tx][k]);
-  if (colsum && ty == 0) {
+  if (gb && threadIdx.x < nout) {
     float s = 0;
-    for (int k = 0; k < 32; ++k) s += tile[k][tx];
-    atomicAdd(&colsum[c0 + tx], s);
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += cs[w][threadIdx.x];
+    atomicAdd(gb + threadIdx.x, s);
   }
 }
 
-// Adam on n parameters; writes the BF16 copies (row-major [nrow][kin] and transposed) for weights
-__global__ void adam_kernel(int n, float* __restrict__ p, float* __restrict__ m, float* __restrict__ v, const float* __restrict__ g,
-                            int gT, int nrow, int kin, float lr, float b1, float b2, float eps, float c1, float c2,
-                            bf16* __restrict__ ph, bf16* __restrict__ pt) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  int r = 0, k = i;
-  if (ph) { r = i / kin; k = i - r * kin; }
-  const float gi = (ph && gT) ? g[(size_t)k * nrow + r] : g[i];
-  const float mi = b1 * m[i] + (1 - b1) * gi, vi = b2 * v[i] + (1 - b2) * gi * gi;
-  m[i] = mi; v[i] = vi;
-  const float pi = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
-  p[i] = pi;
-  if (ph) { ph[i] = __float2bfloat16(pi); pt[(size_t)k * nrow + r] = __float2bfloat16(pi); }
+// Adam over every parameter in one launch.  A segment is one layer's weights (with BF16 copies
+// [nrow][kin] and [kin][nrow]; its gradient possibly transposed) or biases; `start` is its first
+// index in the concatenation.  The bias corrections use the device step counter.
+struct AdamSeg {
+  float *p, *m, *v;
+  const float* g;
+  bf16 *ph, *pt;
+  long long start;
+  int n, gT, nrow, kin;
+};
+
+__global__ void adam_all(const AdamSeg* __restrict__ segs, int nseg, long long total, const long long* __restrict__ step,
+                         const float* __restrict__ lr, float b1, float b2, float eps) {
+  const float t = (float)*step, rate = *lr;
+  const float c1 = 1.0f / (1.0f - exp2f(t * log2f(b1))), c2 = 1.0f / (1.0f - exp2f(t * log2f(b2)));
+  int q = 0;  // a thread's indices increase, so its segment index only moves forward
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    while (q + 1 < nseg && segs[q + 1].start <= e) ++q;
+    const AdamSeg& S = segs[q];
+    const int i = (int)(e - S.start);
+    int r = 0, k = i;
+    if (S.ph) { r = i / S.kin; k = i - r * S.kin; }
+    const float gi = (S.ph && S.gT) ? S.g[(size_t)k * S.nrow + r] : S.g[i];
+    const float mi = b1 * S.m[i] + (1 - b1) * gi, vi = b2 * S.v[i] + (1 - b2) * gi * gi;
+    S.m[i] = mi; S.v[i] = vi;
+    const float pi = S.p[i] - rate * (mi * c1) / (sqrtf(vi * c2) + eps);
+    S.p[i] = pi;
+    if (S.ph) { S.ph[i] = __float2bfloat16(pi); S.pt[(size_t)k * S.nrow + r] = __float2bfloat16(pi); }
+  }
 }
 
 __global__ void to_bf16(int n, const float* __restrict__ p, int nrow, int kin, bf16* __restrict__ ph, bf16* __restrict__ pt) {
@@ -188,8 +231,11 @@ void free_all(sbz_surrogate* s) {
       if (p) cudaFree(p);
   for (auto* v : {&s->X, &s->Z, &s->Xt, &s->dZ, &s->dZt})
     for (bf16* p : *v) if (p) cudaFree(p);
-  for (void* p : {(void*)s->Yf, (void*)s->dY, (void*)s->dYt, (void*)s->T, (void*)s->loss, (void*)s->err, (void*)s->dataX, (void*)s->dataY})
+  for (void* p : {(void*)s->Yf, (void*)s->dY, (void*)s->dYt, (void*)s->T, (void*)s->loss, (void*)s->err, (void*)s->dataX, (void*)s->dataY,
+                  (void*)s->dstep, (void*)s->dlr, s->segs})
     if (p) cudaFree(p);
+  if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+  if (s->graph) cudaGraphDestroy(s->graph);
   if (s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -202,56 +248,79 @@ int refresh_bf16(sbz_surrogate* s) {
 }
 
 int gemm(sbz_surrogate* s, int M, int N, int K, const bf16* A, const bf16* B, int epi, int act, const float* bias, void* out, int ldo,
-         int n_valid, int acc, bf16* z_out, const bf16* z_in) {
+         int n_valid, int acc, bf16* z_out, const bf16* z_in, bf16* out_t = nullptr, float* colsum = nullptr) {
   using namespace sbz::mlp;
   GemmArgs g{};
   g.M = M; g.N = N; g.K = K; g.epi = epi; g.act = act; g.bias = bias;
   g.out_bf16 = static_cast<bf16*>(out); g.out_f32 = static_cast<float*>(out); g.ldo = ldo; g.n_valid = n_valid; g.accumulate = acc;
   g.z_out = z_out; g.z_in = z_in; g.err = s->err;
+  g.out_t = out_t; g.ldt = M; g.colsum = colsum;
   const int r = sbz::mlp::gemm(g, A, B, s->stream);
   return r == SBZ_OK ? SBZ_OK : F(r, "surrogate: GEMM launch");
 }
 
-// forward pass of `rows` (multiple of 128, ≤ batch) rows already in X[0]; result in Yf
-int forward(sbz_surrogate* s, int rows) {
+// forward pass of `rows` (multiple of 128, ≤ batch) rows already in X[0]; result in Yf.  With
+// `train`, the transposed activations X_lᵀ (row stride `rows`) are written for the backward pass.
+int forward(sbz_surrogate* s, int rows, bool train) {
   using namespace sbz::mlp;
   const int nl = (int)s->L.size();
   for (int l = 0; l < nl - 1; ++l) {
     const Layer& y = s->L[l];
-    int r = gemm(s, rows, y.nrow, y.kin, s->X[l], y.Wh, EPI_ACT, ACT_SILU, y.b, s->X[l + 1], y.nrow, y.nrow, 0, s->Z[l + 1], nullptr);
+    int r = gemm(s, rows, y.nrow, y.kin, s->X[l], y.Wh, EPI_ACT, ACT_SILU, y.b, s->X[l + 1], y.nrow, y.nrow, 0, s->Z[l + 1], nullptr,
+                 train ? s->Xt[l + 1] : nullptr);
     if (r) return r;
   }
   const Layer& o = s->L[nl - 1];
   return gemm(s, rows, o.nrow, o.kin, s->X[nl - 1], o.Wh, EPI_F32, ACT_NONE, nullptr, s->Yf, kPadOut, kPadOut, 0, nullptr, nullptr);
 }
 
-// backward pass after forward + loss_grad (dY set); gradients into gW/gb
+// backward pass after forward(train) + loss_grad (dY, dYᵀ and the output layer's gb set): weight
+// gradients into gW, bias gradients accumulated into gb by the EPI_DACT epilogues
 int backward(sbz_surrogate* s) {
   using namespace sbz::mlp;
   const int B = s->batch, nl = (int)s->L.size();
-  const dim3 tb(32, 8);
-  for (auto& l : s->L) SCU(cudaMemsetAsync(l.gb, 0, sizeof(float) * l.nrow, s->stream));
-  // output layer: dW_Lᵀ = X_{L-1}ᵀ dY ([kin][64]); db_L = Σ dY; dZ_{L-1} = (dY W_L) ⊙ SiLU'(Z_{L-1})
+  // output layer: dW_Lᵀ = X_{L-1}ᵀ dY ([kin][64]); dZ_{L-1} = (dY W_L) ⊙ SiLU'(Z_{L-1})
   Layer& o = s->L[nl - 1];
-  transpose_bf16<<<dim3(kPadOut / 32, B / 32), tb, 0, s->stream>>>(B, kPadOut, s->dY, s->dYt, o.gb);
-  transpose_bf16<<<dim3(o.kin / 32, B / 32), tb, 0, s->stream>>>(B, o.kin, s->X[nl - 1], s->Xt[nl - 1], nullptr);
   int r = gemm(s, o.kin, kPadOut, B, s->Xt[nl - 1], s->dYt, EPI_F32, ACT_NONE, nullptr, o.gW, kPadOut, kPadOut, 0, nullptr, nullptr);
   if (r) return r;
-  r = gemm(s, B, o.kin, kPadOut, s->dY, o.Wt, EPI_DACT, ACT_SILU, nullptr, s->dZ[nl - 1], o.kin, o.kin, 0, nullptr, s->Z[nl - 1]);
+  r = gemm(s, B, o.kin, kPadOut, s->dY, o.Wt, EPI_DACT, ACT_SILU, nullptr, s->dZ[nl - 1], o.kin, o.kin, 0, nullptr, s->Z[nl - 1],
+           s->dZt[nl - 1], s->L[nl - 2].gb);
   if (r) return r;
   // hidden layers l = nl-2 .. 0: input X[l], output gradient dZ[l+1]
   for (int l = nl - 2; l >= 0; --l) {
     Layer& y = s->L[l];
-    transpose_bf16<<<dim3(y.nrow / 32, B / 32), tb, 0, s->stream>>>(B, y.nrow, s->dZ[l + 1], s->dZt[l + 1], y.gb);
-    transpose_bf16<<<dim3(y.kin / 32, B / 32), tb, 0, s->stream>>>(B, y.kin, s->X[l], s->Xt[l], nullptr);
     r = gemm(s, y.nrow, y.kin, B, s->dZt[l + 1], s->Xt[l], EPI_F32, ACT_NONE, nullptr, y.gW, y.kin, y.kin, 0, nullptr, nullptr);
     if (r) return r;
     if (l > 0) {
-      r = gemm(s, B, y.kin, y.nrow, s->dZ[l + 1], y.Wt, EPI_DACT, ACT_SILU, nullptr, s->dZ[l], y.kin, y.kin, 0, nullptr, s->Z[l]);
+      r = gemm(s, B, y.kin, y.nrow, s->dZ[l + 1], y.Wt, EPI_DACT, ACT_SILU, nullptr, s->dZ[l], y.kin, y.kin, 0, nullptr, s->Z[l], s->dZt[l],
+               s->L[l - 1].gb);
       if (r) return r;
     }
   }
   return cudaGetLastError() == cudaSuccess ? SBZ_OK : F(SBZ_ERR_CUDA, "surrogate: backward");
+}
+
+// forward + loss + backward of the `rows` rows in X[0] (and X[0]ᵀ) with targets T
+int forward_backward(sbz_surrogate* s, int rows) {
+  int r = forward(s, rows, true);
+  if (r) return r;
+  for (auto& l : s->L) SCU(cudaMemsetAsync(l.gb, 0, sizeof(float) * l.nrow, s->stream));
+  loss_grad<<<(rows + kLossThreads - 1) / kLossThreads, kLossThreads, 0, s->stream>>>(rows, s->nout, s->Yf, s->L.back().b, s->T, s->dY, s->dYt,
+                                                                                  s->L.back().gb, s->loss);
+  return backward(s);
+}
+
+// one training step on the stream (captured into the step graph)
+int train_step(sbz_surrogate* s) {
+  const int B = s->batch;
+  begin_step<<<1, 1, 0, s->stream>>>(s->dstep, s->loss);
+  gather_batch<<<(B + 127) / 128, 128, 0, s->stream>>>(B, s->nin, s->nout, s->dataX, s->dataY, s->ndata, 0, s->dstep, s->seed, 0, 1, s->X[0],
+                                                      s->Xt[0], s->T);
+  int r = forward_backward(s, B);
+  if (r) return r;
+  adam_all<<<2 * 152, 256, 0, s->stream>>>(static_cast<const AdamSeg*>(s->segs), s->nseg, s->nparam_all, s->dstep, s->dlr, 0.9f, 0.999f,
+                                           1e-8f);
+  return cudaGetLastError() == cudaSuccess ? SBZ_OK : F(SBZ_ERR_CUDA, "surrogate: training step");
 }
 
 int check_err(sbz_surrogate* s) {
@@ -316,6 +385,23 @@ int sbz_surrogate_create(int nin, int width, int nhidden, int nout, int batch, u
       dalloc(&s->T, (size_t)batch * nout) || dalloc(&s->loss, 1) || dalloc(&s->err, 1))
     return bail("surrogate: buffer allocation");
   cudaMemset(s->err, 0, sizeof(unsigned));
+  {
+    std::vector<AdamSeg> segs;
+    long long start = 0;
+    for (auto& l : s->L) {
+      const int n = l.nrow * l.kin;
+      segs.push_back(AdamSeg{l.W, l.mW, l.vW, l.gW, l.Wh, l.Wt, start, n, l.gT ? 1 : 0, l.nrow, l.kin});
+      start += n;
+      segs.push_back(AdamSeg{l.b, l.mb, l.vb, l.gb, nullptr, nullptr, start, l.nrow, 0, l.nrow, 1});
+      start += l.nrow;
+    }
+    s->nseg = (int)segs.size();
+    s->nparam_all = start;
+    if (dalloc(&s->dstep, 1) || dalloc(&s->dlr, 1) || cudaMalloc(&s->segs, sizeof(AdamSeg) * segs.size()) != cudaSuccess)
+      return bail("surrogate: buffer allocation");
+    cudaMemcpy(s->segs, segs.data(), sizeof(AdamSeg) * segs.size(), cudaMemcpyHostToDevice);
+    cudaMemset(s->dstep, 0, sizeof(long long));
+  }
   if (refresh_bf16(s) != SBZ_OK) { free_all(s); delete s; return SBZ_ERR_CUDA; }
   if (cudaStreamSynchronize(s->stream) != cudaSuccess) return bail("surrogate: initialisation");
   *out = s;
@@ -364,6 +450,9 @@ int sbz_surrogate_set_params(sbz_surrogate* s, const float* params) {
 
 int sbz_surrogate_set_data(sbz_surrogate* s, long long n, const float* X, const float* Y) {
   if (!s || n < 1 || !X || !Y) return F(SBZ_ERR_ARG, "sbz_surrogate_set_data: bad arguments");
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->graph_exec) { cudaGraphExecDestroy(s->graph_exec); s->graph_exec = nullptr; }
+  if (s->graph) { cudaGraphDestroy(s->graph); s->graph = nullptr; }
   if (s->dataX) cudaFree(s->dataX);
   if (s->dataY) cudaFree(s->dataY);
   s->dataX = s->dataY = nullptr;
@@ -378,27 +467,27 @@ int sbz_surrogate_set_data(sbz_surrogate* s, long long n, const float* X, const 
 int sbz_surrogate_train(sbz_surrogate* s, int nsteps, double lr, double* loss_out) {
   if (!s || nsteps < 0 || !(lr > 0)) return F(SBZ_ERR_ARG, "sbz_surrogate_train: bad arguments");
   if (!s->dataX) return F(SBZ_ERR_STATE, "sbz_surrogate_train: no training data (sbz_surrogate_set_data)");
-  const int B = s->batch;
-  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-  for (int it = 0; it < nsteps; ++it) {
+  set_value<<<1, 1, 0, s->stream>>>(s->dlr, (float)lr);
+  int r = SBZ_OK;
+  if (!s->graph_exec && nsteps > 0) {
+    // the first step runs eagerly (kernel attributes, tensor-map encoder), the next is captured
+    if ((r = train_step(s))) return r;
     ++s->step;
-    gather_batch<<<(B + 127) / 128, 128, 0, s->stream>>>(B, s->nin, s->nout, s->dataX, s->dataY, s->ndata, s->step, s->seed, 0, 1, s->X[0], s->T);
-    int r = forward(s, B);
-    if (r) return r;
-    SCU(cudaMemsetAsync(s->loss, 0, sizeof(double), s->stream));
-    const Layer& o = s->L.back();
-    loss_grad<<<(B + 255) / 256, 256, 0, s->stream>>>(B, s->nout, s->Yf, o.b, s->T, s->dY, s->loss);
-    if ((r = backward(s))) return r;
-    const float c1 = 1.0f / (1.0f - std::pow(b1, (float)s->step)), c2 = 1.0f / (1.0f - std::pow(b2, (float)s->step));
-    for (auto& l : s->L) {
-      const int n = l.nrow * l.kin;
-      adam_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(n, l.W, l.mW, l.vW, l.gW, l.gT, l.nrow, l.kin, (float)lr, b1, b2, eps, c1, c2, l.Wh,
-                                                          l.Wt);
-      adam_kernel<<<(l.nrow + 255) / 256, 256, 0, s->stream>>>(l.nrow, l.b, l.mb, l.vb, l.gb, 0, l.nrow, 1, (float)lr, b1, b2, eps, c1, c2,
-                                                               nullptr, nullptr);
+    --nsteps;
+    SCU(cudaStreamSynchronize(s->stream));
+    SCU(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    r = train_step(s);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+    if (r || e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return r ? r : F(SBZ_ERR_CUDA, std::string("surrogate: step capture: ") + cudaGetErrorString(e));
     }
-    SCU(cudaGetLastError());
+    s->graph = g;
+    SCU(cudaGraphInstantiate(&s->graph_exec, s->graph, 0));
   }
+  for (int it = 0; it < nsteps; ++it) SCU(cudaGraphLaunch(s->graph_exec, s->stream));
+  s->step += nsteps;
   if (loss_out) SCU(cudaMemcpyAsync(loss_out, s->loss, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
   return check_err(s);
 }
@@ -414,13 +503,9 @@ int sbz_surrogate_gradients(sbz_surrogate* s, int n, const float* X, const float
   SCU(dalloc(&dy, (size_t)n * s->nout));
   SCU(cudaMemcpy(dx, X, sizeof(float) * n * s->nin, cudaMemcpyHostToDevice));
   SCU(cudaMemcpy(dy, Y, sizeof(float) * n * s->nout, cudaMemcpyHostToDevice));
-  gather_batch<<<(n + 127) / 128, 128, 0, s->stream>>>(n, s->nin, s->nout, dx, dy, n, 0, 0, 0, 0, s->X[0], s->T);
-  int r = forward(s, n);
-  if (!r) {
-    cudaMemsetAsync(s->loss, 0, sizeof(double), s->stream);
-    loss_grad<<<(n + 255) / 256, 256, 0, s->stream>>>(n, s->nout, s->Yf, s->L.back().b, s->T, s->dY, s->loss);
-    r = backward(s);
-  }
+  gather_batch<<<(n + 127) / 128, 128, 0, s->stream>>>(n, s->nin, s->nout, dx, dy, n, 0, nullptr, 0, 0, 0, s->X[0], s->Xt[0], s->T);
+  cudaMemsetAsync(s->loss, 0, sizeof(double), s->stream);
+  int r = forward_backward(s, n);
   s->batch = keepB;
   cudaFree(dx); cudaFree(dy);
   if (r) return r;
@@ -455,8 +540,9 @@ int sbz_surrogate_infer(sbz_surrogate* s, long long n, const float* X, float* Y)
     for (long long b0 = 0; b0 < cn && !r; b0 += B) {
       const int rows = (int)std::min<long long>(B, cn - b0);
       const int prow = (rows + 127) / 128 * 128;
-      gather_batch<<<(prow + 127) / 128, 128, 0, s->stream>>>(prow, s->nin, s->nout, dx + b0 * s->nin, nullptr, rows, 0, 0, 0, 0, s->X[0], nullptr);
-      if ((r = forward(s, prow))) break;
+      gather_batch<<<(prow + 127) / 128, 128, 0, s->stream>>>(prow, s->nin, s->nout, dx + b0 * s->nin, nullptr, rows, 0, nullptr, 0, 0, 0, s->X[0],
+                                                              nullptr, nullptr);
+      if ((r = forward(s, prow, false))) break;
       add_bias_out<<<(rows * s->nout + 255) / 256, 256, 0, s->stream>>>(rows, s->nout, s->Yf, s->L.back().b, dyo);
       if (cudaMemcpyAsync(Y + (c0 + b0) * s->nout, dyo, sizeof(float) * rows * s->nout, cudaMemcpyDeviceToHost, s->stream) != cudaSuccess)
         r = SBZ_ERR_CUDA;
