@@ -59,10 +59,10 @@ int launch(const GemmArgs& g, const void* A, const void* B, cudaStream_t st) {
     attr_set = true;
   }
   const int tiles = (g.N / BN) * (g.M / BM), KT = g.K / BK;
-  // weight gradients have few output tiles and a long K (the batch): split K over about one CTA
+  // weight gradients have few output tiles and a long K (the batch): split K over about two CTAs
   // per SM, at least 4 K-steps each, and add the partial tiles atomically into a zeroed output
   int splits = 1;
-  if (g.epi == EPI_F32 && tiles < num_sms()) splits = std::max(1, std::min(KT / 4, num_sms() / tiles));
+  if (g.epi == EPI_F32 && tiles < 2 * num_sms()) splits = std::max(1, std::min(KT / 4, 2 * num_sms() / tiles));
   if (splits > 1 && !g.accumulate) {
     for (int r = 0; r < g.M; ++r) {  // rows of the output region (ldo may exceed N)
       if (g.ldo == g.n_valid) {

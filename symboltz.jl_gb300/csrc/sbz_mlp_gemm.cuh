@@ -2,8 +2,10 @@
 //
 //   D[M x N] = A[M x K] · B[N x K]ᵀ   (A, B bf16 row-major with K contiguous, FP32 accumulation)
 //
-// One CTA computes a 128 x BN tile.  Warp 0 lane 0 streams 128 x 64 and BN x 64 K-slices into a
-// four-stage shared-memory ring with TMA (128-byte swizzle); warp 1 lane 0 issues
+// One CTA computes a 128 x BN tile; two CTAs share an SM (≈ 100 KB of shared memory and at most
+// 128 registers per thread each), so one CTA's epilogue overlaps the other's loads.  Warp 0 lane 0
+// streams 128 x 64 and BN x 64 K-slices into a shared-memory ring of stages_for<BN>() slots with
+// TMA (128-byte swizzle); warp 1 lane 0 issues
 // tcgen05.mma (kind::f16, M = 128, N = BN, K = 16) into a TMEM accumulator and releases ring
 // slots with tcgen05.commit; all eight warps then read the accumulator with tcgen05.ld (warp w owns
 // TMEM lanes 32(w mod 4).. = tile rows, and half w / 4 of the tile's columns) and apply the fused
@@ -25,7 +27,9 @@
 namespace sbz {
 namespace mlp {
 
-constexpr int BM = 128, BK = 64, STAGES = 4, kThreads = 256;
+constexpr int BM = 128, BK = 64, kThreads = 256;
+template <int BN>
+__host__ __device__ constexpr int stages_for() { return BN >= 256 ? 2 : BN >= 128 ? 3 : 4; }  // (BM + BN) · BK · 2 B · stages ≤ 96 KB
 constexpr unsigned kWaitLimit = 1u << 24;
 enum { EPI_F32 = 0, EPI_ACT = 1, EPI_DACT = 2 };
 enum { ACT_NONE = 0, ACT_SILU = 1 };
@@ -49,6 +53,7 @@ struct GemmArgs {
 
 template <int BN>
 constexpr size_t gemm_smem_bytes() {
+  constexpr int STAGES = stages_for<BN>();
   return 1024 /* alignment slack */ + (size_t)STAGES * (BM + BN) * BK * 2 + (2 * STAGES + 1) * 8 + 16 + BN * 4 /* bias */;
 }
 
@@ -148,8 +153,9 @@ __device__ __forceinline__ void store_transposed(const unsigned (&yp)[16], __nv_
 }
 
 template <int BN>
-__global__ void __launch_bounds__(kThreads, 1) gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA,
+__global__ void __launch_bounds__(kThreads, 2) gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA,
                                                          const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
+  constexpr int STAGES = stages_for<BN>();
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* sA = base;
