@@ -402,7 +402,10 @@ def run_surrogate(args):
             "fallback_rate": float(fb.mean()), "tol_probe": args.surrogate_tol,
             "probe_error": {"median": float(np.median(errs)), "max": float(np.max(errs))},
             "cl_max_rel_vs_fp64": {"with_fallback": {"median": float(np.median(rel.max(axis=1))), "max": float(rel.max())},
-                                   "surrogate_only": {"median": float(np.median(rel_raw.max(axis=1))), "max": float(rel_raw.max())}},
+                                   "surrogate_only": {"median": float(np.median(rel_raw.max(axis=1))), "max": float(rel_raw.max()),
+                                                      "median_by_spectrum": dict(zip(("TT", "TE", "EE"),
+                                                                                     np.median(rel_raw, axis=0).round(6).tolist()))}},
+            "estimate_vs_true_surrogate_error": [[round(float(e), 6), round(float(t), 6)] for e, t in zip(errs, rel_raw.max(axis=1))],
             "training": {"cosmologies": args.train_cosmologies, "samples": int(args.train_cosmologies * len(ks) * sur.ntau),
                          "data_s": round(t_data, 2), "steps": steps, "train_s": round(t_train, 2),
                          "tflops": round(steps * flops_step / t_train / 1e12, 1), "batch": 65536,
@@ -414,8 +417,23 @@ def run_surrogate(args):
 def profile_case(args):
     """Small cases for ncu section captures.  pt: 64 of the 1000 modes (even in log k, the slowest
     included), sources on 200 times.  los: one spectrum_cmb of the full workload (the line-of-sight
-    kernel runs once on the full fine k grid; ~1.5 GB on the device)."""
+    kernel runs once on the full fine k grid; ~1.5 GB on the device).  mlp: the surrogate's training
+    step (8 -> 4x512 -> 7, batch 65536) on 2 M synthetic samples, one eager step, the graph capture
+    and 4 graph replays, plus a timed run of 200 steps printed first."""
     import symboltz as S
+    if args.profile_case == "mlp":
+        from symboltz.surrogate import MLP
+        rng = np.random.default_rng(0)
+        net = MLP(8, 512, 4, 7, 65536, 0)
+        net.set_data(rng.uniform(-1, 1, (2_000_000, 8)).astype(np.float32), rng.normal(size=(2_000_000, 7)).astype(np.float32))
+        net.train(5, 1e-3)
+        if args.steps > 5:
+            t0 = time.perf_counter()
+            net.train(args.steps, 1e-3)
+            dt = time.perf_counter() - t0
+            print(json.dumps({"profile_case": "mlp training step", "steps": args.steps, "ms_per_step": round(dt / args.steps * 1e3, 4),
+                              "tflops": round(3 * 2 * 65536 * (64 * 512 + 3 * 512 * 512 + 512 * 64) * args.steps / dt / 1e12, 1)}))
+        return
     M = S.ΛCDM(lmax_gamma=MODEL["lmax_gamma"], lmax_nu=MODEL["lmax_nu"], lmax_h=MODEL["lmax_h"], nx=MODEL["nx"])
     prob = S.CosmologyProblem(M, PARAMS, precision=args.precision)
     ks, taus, ls = workload_grids(S, prob)
@@ -442,10 +460,10 @@ def main():
     ap.add_argument("--train-cosmologies", type=int, default=64)
     ap.add_argument("--train-seconds", type=float, default=120.0)
     ap.add_argument("--test-cosmologies", type=int, default=16)
-    ap.add_argument("--surrogate-tol", type=float, default=0.05)
+    ap.add_argument("--surrogate-tol", type=float, default=1e-3)
     ap.add_argument("--workload", choices=("spectrum", "batched", "surrogate"), default="spectrum",
                     help="spectrum: the headline single-cosmology C_l workload; batched: 256 cosmologies, ragged k grids")
-    ap.add_argument("--profile-case", choices=("pt", "los"), default=None,
+    ap.add_argument("--profile-case", choices=("pt", "los", "mlp"), default=None,
                     help="small cases for ncu section captures (see profile_case)")
     args = ap.parse_args()
     if args.profile_case:

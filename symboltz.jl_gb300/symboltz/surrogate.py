@@ -6,9 +6,11 @@ each cosmology's visibility function.  It is trained on factors computed by the 
 solver (output "factors") with the library's own BF16 tensor-core forward/backward kernels
 (``sbz_surrogate_*``), and evaluated the same way.
 Its sources go through the regular k-interpolation → line-of-sight → C_ℓ pipeline
-(``sbz_spectrum_cmb_sources``).  Each cosmology gets an error estimate from a few probe modes that
-are also solved with the real solver; a cosmology whose probes disagree by more than the tolerance is
-recomputed with the solver (fallback), which therefore remains the judge of every result.
+(``sbz_spectrum_cmb_sources``).  Each cosmology gets an error estimate in the C_ℓ metric: 48 probe
+modes are also solved with the real solver, and D_ℓ from the surrogate's and the solver's sources
+at those modes (same pipeline, same probe grid) are compared; a cosmology whose estimate exceeds
+the tolerance is recomputed with the solver (fallback), which therefore remains the judge of every
+result.
 """
 import ctypes as C
 
@@ -133,6 +135,8 @@ class SourceSurrogate:
         self.net = MLP(8, width, nhidden, 7, batch, seed)
         self.mean = np.zeros(7)
         self.scale = np.ones(7)
+        self.env_lk = np.array([-1.0, 1.0])  # k envelope: log k feature nodes and log RMS per factor
+        self.env_la = np.zeros((2, 7))
 
     # ---- features, background, targets ------------------------------------------------------
     def features(self, theta, taus, ks=None):
@@ -227,12 +231,28 @@ class SourceSurrogate:
         return X, Y, taus
 
     # ---- training ---------------------------------------------------------------------------
+    def envelope(self, lk):
+        """RMS amplitude of each target at the log-k features lk [n, 7] (log-linear between the
+        training grid's k), so the network learns every k to the same relative accuracy: the
+        Silk-damped high-k factors are orders of magnitude below the low-k ones."""
+        return np.exp(np.stack([np.interp(lk, self.env_lk, self.env_la[:, j]) for j in range(7)], axis=1))
+
+    def normalise(self, X, Y):
+        return (Y / self.envelope(X[:, 6]) - self.mean) / self.scale
+
     def fit(self, X, Y, steps, lr=1e-3, lr_final=1e-5, chunks=20):
-        """Standardise the targets and train `steps` Adam steps with an exponential learning-rate
-        decay from lr to lr_final; returns the loss after each chunk."""
-        self.mean = Y.mean(axis=0)
-        self.scale = Y.std(axis=0) + 1e-30
-        self.net.set_data(X, (Y - self.mean) / self.scale)
+        """Divide the targets by their k envelope, standardise, and train `steps` Adam steps with an
+        exponential learning-rate decay from lr to lr_final; returns the loss after each chunk."""
+        lk, inv = np.unique(X[:, 6].astype(np.float64), return_inverse=True)
+        cnt = np.bincount(inv, minlength=len(lk)).astype(np.float64)
+        ms = np.stack([np.bincount(inv, weights=Y[:, j].astype(np.float64) ** 2, minlength=len(lk)) for j in range(7)], axis=1) / cnt[:, None]
+        rms = np.sqrt(ms)
+        rms = np.maximum(rms, 1e-12 * rms.max(axis=0, keepdims=True) + 1e-300)
+        self.env_lk, self.env_la = lk, np.log(rms)
+        Z = Y / self.envelope(X[:, 6])
+        self.mean = Z.mean(axis=0)
+        self.scale = Z.std(axis=0) + 1e-30
+        self.net.set_data(X, ((Z - self.mean) / self.scale).astype(np.float32))
         losses = []
         per = max(1, steps // chunks)
         done = 0
@@ -246,12 +266,13 @@ class SourceSurrogate:
     def mse(self, X, Y):
         """Mean squared error of the network on (X, Y) in standardised units (all rows)."""
         P = self.net.infer(X).astype(np.float64)
-        return float(np.mean((P - (Y - self.mean) / self.scale) ** 2))
+        return float(np.mean((P - self.normalise(X, Y)) ** 2))
 
     # ---- prediction ------------------------------------------------------------------------
     def predict_factors(self, theta, taus, vis, ks=None):
         ks = self.ks if ks is None else np.asarray(ks, dtype=np.float64)
-        G = (self.net.infer(self.features(theta, taus, ks)).astype(np.float64) * self.scale + self.mean).reshape(len(ks), len(taus), 7)
+        X = self.features(theta, taus, ks)
+        G = ((self.net.infer(X).astype(np.float64) * self.scale + self.mean) * self.envelope(X[:, 6])).reshape(len(ks), len(taus), 7)
         return self.from_targets(G, ks, vis)
 
     def predict_sources(self, theta, taus, vis, ks=None):
@@ -260,23 +281,40 @@ class SourceSurrogate:
 
     def save(self, path):
         self.net.save(path)
-        np.savez(str(path) + ".norm.npz", mean=self.mean, scale=self.scale, ks=self.ks, ntau=self.ntau)
+        np.savez(str(path) + ".norm.npz", mean=self.mean, scale=self.scale, env_lk=self.env_lk, env_la=self.env_la, ks=self.ks,
+                 ntau=self.ntau)
 
-    def probe_error(self, theta, taus, vis, F_true, kprobe):
-        """Relative L2 error of the predicted sources (k S_T, k² S_E) against the solver's at the
-        probe modes."""
-        P = self.predict_sources(theta, taus, vis, kprobe)[..., :2]
-        T = self.sources(F_true, kprobe, taus, vis)[..., :2]
-        return float(np.linalg.norm(P - T) / (np.linalg.norm(T) + 1e-300))
+    @staticmethod
+    def cl_error(D, ref):
+        """Largest relative difference of D_ℓ [nl, 3] (TT, TE, EE) from ref over ℓ and modes, TE
+        relative to sqrt(TT EE) — the metric the C_ℓ tolerance is stated in."""
+        den = np.stack([np.abs(ref[:, 0]), np.sqrt(np.abs(ref[:, 0] * ref[:, 2])), np.abs(ref[:, 2])], axis=1)
+        return float(np.max(np.abs(D - ref) / np.where(den > 0, den, np.inf)))
 
-    def spectra(self, thetas, jl, ls_out, kinterp, modes=("TT", "TE", "EE"), tol=0.05, kprobe=None, fallback=True):
+    def probe_kgrid(self, nprobe=48):
+        """Probe modes: an even subset of the coarse grid, both ends included."""
+        idx = np.unique(np.round(np.linspace(0, len(self.ks) - 1, nprobe)).astype(int))
+        return self.ks[idx]
+
+    def probe_error(self, theta, taus, vis, F_true, kprobe, prob, cosmo, jl, ls_out):
+        """Held-out error estimate in the C_ℓ metric: D_ℓ from the surrogate's sources and from the
+        solver's sources at the probe modes, both through the same line-of-sight pipeline on the
+        probe grid (its coarseness is common to both and cancels in the difference)."""
+        from . import CubicSplineInterpolator, spectrum_cmb
+        kin = CubicSplineInterpolator(kprobe, f=np.log)
+        run = lambda src: spectrum_cmb(["TT", "TE", "EE"], prob, jl, ls_out, kinterp=kin, taus=taus, cosmo=cosmo,  # noqa: E731
+                                       normalization="Dl", sources=src)
+        ref = run(self.sources(F_true, kprobe, taus, vis))
+        return self.cl_error(run(self.predict_sources(theta, taus, vis, kprobe)), ref)
+
+    def spectra(self, thetas, jl, ls_out, kinterp, modes=("TT", "TE", "EE"), tol=1e-3, kprobe=None, fallback=True):
         """C_ℓ (D_ℓ) for each θ: surrogate sources through the line-of-sight pipeline, or the solver
-        for cosmologies whose probe-mode error exceeds tol.  Returns (Dl [ncos][nl][nmodes], probe
-        errors, fallback mask)."""
+        for cosmologies whose held-out error estimate (probe_error, relative D_ℓ) exceeds tol.
+        Returns (Dl [ncos][nl][nmodes], error estimates, fallback mask)."""
         from . import CosmologyProblem, spectrum_cmb
-        kprobe = np.geomspace(self.ks.min() * 10, self.ks.max() / 3, 4) if kprobe is None else np.asarray(kprobe)
+        kprobe = self.probe_kgrid() if kprobe is None else np.asarray(kprobe)
         Fp, taus, vis, prob = self.solve_factors(thetas, ks=kprobe)
-        errs = np.array([self.probe_error(t, taus[c], vis[c], Fp[c], kprobe) for c, t in enumerate(thetas)])
+        errs = np.array([self.probe_error(t, taus[c], vis[c], Fp[c], kprobe, prob, c, jl, ls_out) for c, t in enumerate(thetas)])
         fb = (errs > tol) if fallback else np.zeros(len(thetas), dtype=bool)
         out = []
         for c, t in enumerate(thetas):
