@@ -79,7 +79,6 @@ struct ModeMem {
   ST hmul[kMaxChains], hcorr[kMaxChains];
   ST wS[kWF], fS[4];  // Jacobian-set functional weights and Φ̇ coefficients in solve precision
   CSet cs[kNSets];
-  double hv[kMaxT][8], hd[kMaxT][8];     // table interpolants per time: a, ℋ, κ̇, c_s², e^{-κ}, κ̈, κ⃛
   double B[kMaxT][B_COUNT], dB[kMaxT][B_COUNT];
   double src[4];      // e^{-κ}, κ̈, κ⃛ at an output time
   double red[2][NW];  // ping-pong group reductions
@@ -101,10 +100,11 @@ struct Grp {
 };
 
 // Component held by thread gt in slot s.  Slot 0 is the identity (the head rows with their extra
-// couplings sit in warp 0); later slots start at the last warp, so the partial last slot does not
-// land on warp 0 as well.
+// couplings sit in warp 0); slot s ≥ 1 is rotated by s·(NW-1) warps, so a partial last slot lands
+// on warp 1 — for NW = 4 the warp of the photon tails, which carries no metric-coupled row and so
+// skips the Ψ/Φ̇ functionals of every operator product — not on the head warp.
 template <int NW>
-__device__ __forceinline__ int comp_of(int gt, int s) { return s * 32 * NW + ((gt + 32 * s) & (32 * NW - 1)); }
+__device__ __forceinline__ int comp_of(int gt, int s) { return s * 32 * NW + ((gt + 32 * (NW - 1) * s) & (32 * NW - 1)); }
 
 // per-lane model constants kept in registers: the lane's functional component and, per slot,
 // whether any row of this warp carries a Φ̇ or Ψ coupling (warp-uniform; the operator products skip
@@ -185,72 +185,93 @@ struct ModeK {  // per-mode constants
 };
 
 // ------------------------------------------------------------------------------------------
+// Cubic Hermite interpolation of table quantity c at τ (value, and τ-derivative if want_d).  The node
+// index comes from an FP32 logarithm and can be one off next to a node: every load of the guessed
+// interval is issued at once and repeated only in that rare case.
+__device__ __forceinline__ void table_hermite(const CosmoDesc* __restrict__ cd, const double* __restrict__ tab, double tau, int c,
+                                              bool want_d, double& val, double& der) {
+  const int ntab = cd->ntab;
+  int gi = (int)((__logf((float)tau) - (float)cd->lnt0) * (float)cd->idlnt);
+  gi = max(0, min(gi, ntab - 2));
+  const double* nd = tab + (size_t)gi * kNodeStride;
+  double t0 = nd[0], t1 = nd[kNodeStride], ih = nd[1];
+  double v0 = nd[2 + 2 * c], d0 = nd[3 + 2 * c], v1 = nd[kNodeStride + 2 + 2 * c], d1 = nd[kNodeStride + 3 + 2 * c];
+  const int shift = (tau < t0 && gi > 0) ? -1 : (tau > t1 && gi < ntab - 2) ? 1 : 0;
+  if (shift) {
+    nd += shift * kNodeStride;
+    t0 = nd[0]; t1 = nd[kNodeStride]; ih = nd[1];
+    v0 = nd[2 + 2 * c]; d0 = nd[3 + 2 * c]; v1 = nd[kNodeStride + 2 + 2 * c]; d1 = nd[kNodeStride + 3 + 2 * c];
+  }
+  const double h = t1 - t0;
+  const double s = (tau - t0) * ih, s2 = s * s, s3 = s2 * s;
+  val = (2 * s3 - 3 * s2 + 1) * v0 + (s3 - 2 * s2 + s) * h * d0 + (3 * s2 - 2 * s3) * v1 + (s3 - s2) * h * d1;
+  der = want_d ? ((6 * s2 - 6 * s) * v0 + (6 * s - 6 * s2) * v1) * ih + (3 * s2 - 4 * s + 1) * d0 + (3 * s2 - 2 * s) * d1 : 0.0;
+}
+
+// ------------------------------------------------------------------------------------------
 // τ-dependent coefficients at nt ≤ kMaxT times into sets cs[set[q]]; derivative sets where bit q
 // of dmask is set.  source = true (nt = 1): also fetch e^{-κ}, κ̈, κ⃛ and use the Taylor-mode κ̈
 // as dκ̇/dτ (the line-of-sight sources differentiate the background along its ODE,
-// src/models/cosmologies.jl:99-105).  Warp 0 interpolates the table and forms the base scalars;
-// the expressions are spread over the group.  The caller guarantees that no thread still reads
-// the target sets; the call ends with a group barrier.
+// src/models/cosmologies.jl:99-105).  The base scalars are formed by four independent roles that
+// run on different warps (folded onto fewer warps when NW < 4), each interpolating the table
+// itself: role 0/1 the seven table quantities of the times without/with derivatives, with 1/a and
+// 1/ℋ; role 2 the momentum-bin energies; role 3 the k constants and 1/τ.  The expressions are then
+// spread over the group.  The caller guarantees that no thread still reads the target sets; the
+// call ends with a group barrier.
 template <int NW, int NSL, typename ST>
 __device__ __forceinline__ void coef_eval(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const int* set, const double* taus, int nt,
-                          unsigned dmask, bool source, const CosmoDesc* __restrict__ cd, const double* __restrict__ tab,
+                          unsigned dmask, bool source, const CosmoDesc* cd, const double* __restrict__ tab,
                           int nexpr, int nx, const ModeK& mk) {
-  if (g.wq == 0) {
-    const int lane = g.lane;
-    // Hermite interpolants: lane = 8 q + quantity (7 quantities per time)
-    {
+  const int lane = g.lane;
+  for (int role = g.wq; role < 4; role += NW) {
+    if (role <= 1) {  // table quantities: lane = 8 q + quantity
       const int q = lane >> 3, c = lane & 7;
-      if (q < nt && c < 7) {
-        const double tau = taus[q];
-        const int ntab = cd->ntab;
-        int gi = (int)((__logf((float)tau) - (float)cd->lnt0) * (float)cd->idlnt);
-        gi = max(0, min(gi, ntab - 2));
-        const double* nd = tab + (size_t)gi * kNodeStride;
-        if (tau < nd[0] && gi > 0) nd -= kNodeStride;
-        else if (tau > nd[kNodeStride] && gi < ntab - 2) nd += kNodeStride;
-        const double t0 = nd[0], ih = nd[1], h = nd[kNodeStride] - t0;
-        const double s = (tau - t0) * ih, s2 = s * s, s3 = s2 * s;
-        const double v0 = nd[2 + 2 * c], d0 = nd[3 + 2 * c], v1 = nd[kNodeStride + 2 + 2 * c], d1 = nd[kNodeStride + 3 + 2 * c];
-        W.hv[q][c] = (2 * s3 - 3 * s2 + 1) * v0 + (s3 - 2 * s2 + s) * h * d0 + (3 * s2 - 2 * s3) * v1 + (s3 - s2) * h * d1;
-        W.hd[q][c] = ((6 * s2 - 6 * s) * v0 + (6 * s - 6 * s2) * v1) * ih + (3 * s2 - 4 * s + 1) * d0 + (3 * s2 - 2 * s) * d1;
+      if (q < nt && c < 7 && (int)((dmask >> q) & 1u) == role) {
+        const bool dq = role == 1;
+        double v, d;
+        table_hermite(cd, tab, taus[q], c, dq, v, d);
+        double* Bq = W.B[q]; double* dBq = W.dB[q];
+        if (c == 0) {  // a: 1/a, 1/a², R = R0/a
+          const double ia = 1.0 / v;
+          Bq[B_IA] = ia; Bq[B_IA2] = ia * ia; Bq[B_R] = cd->R0 * ia;
+          if (dq) { const double dia = -d * ia * ia; dBq[B_IA] = dia; dBq[B_IA2] = 2 * ia * dia; dBq[B_R] = cd->R0 * dia; }
+        } else if (c == 1) {  // ℋ and 1/ℋ
+          const double ih = 1.0 / v;
+          Bq[B_H] = v; Bq[B_IH] = ih;
+          if (dq) { dBq[B_H] = d; dBq[B_IH] = -d * ih * ih; }
+        } else if (c == 2) {  // κ̇
+          Bq[B_KD] = v;
+          if (dq && !source) dBq[B_KD] = d;
+        } else if (c == 3) {  // c_s²
+          Bq[B_CS2] = v;
+          if (dq) dBq[B_CS2] = d;
+        } else {  // e^{-κ}, κ̈, κ⃛: line-of-sight sources only (κ̈ is then dκ̇/dτ)
+          if (source) W.src[c - 4] = v;
+          if (source && c == 5) dBq[B_KD] = v;
+        }
       }
-    }
-    __syncwarp();
-    // reciprocals and momentum-bin energies: entry p = (3 + nx) q + j, j = 0: a, 1: τ, 2: ℋ, 3 + b: E_b
-    const int per = 3 + nx;
-    for (int p = lane; p < nt * per; p += 32) {
-      const int q = p / per, j = p - q * per;
-      const double a = W.hv[q][0], da = W.hd[q][0];
-      double rv, drv;
-      if (j == 0) { rv = a; drv = da; }
-      else if (j == 1) { rv = taus[q]; drv = 1.0; }
-      else if (j == 2) { rv = W.hv[q][1]; drv = W.hd[q][1]; }
-      else {
-        const int b = j - 3;
+    } else if (role == 2) {  // momentum-bin energies E_b = sqrt(x_b² + (y0 a)²): lane = 8 q + b
+      const int q = lane >> 3, b = lane & 7;
+      if (q < nt && b < nx) {
+        const bool dq = (dmask >> q) & 1u;
+        double a, da;
+        table_hermite(cd, tab, taus[q], 0, dq, a, da);
         const double xj = cd->xq[b], y0a = cd->y0 * a;
         const double E2 = xj * xj + y0a * y0a;
         const double iE = rsqrt(E2), E = E2 * iE;
-        const double dE = cd->y0 * y0a * da * iE;
         const double ixj = cd->ixq[b];
         W.B[q][B_Q + b] = xj * iE; W.B[q][B_IQ + b] = E * ixj; W.B[q][B_E + b] = E; W.B[q][B_IE + b] = iE;
-        W.dB[q][B_Q + b] = -xj * dE * iE * iE; W.dB[q][B_IQ + b] = dE * ixj; W.dB[q][B_E + b] = dE; W.dB[q][B_IE + b] = -dE * iE * iE;
-        continue;
+        if (dq) {
+          const double dE = cd->y0 * y0a * da * iE;
+          W.dB[q][B_Q + b] = -xj * dE * iE * iE; W.dB[q][B_IQ + b] = dE * ixj; W.dB[q][B_E + b] = dE; W.dB[q][B_IE + b] = -dE * iE * iE;
+        }
       }
-      const double inv = 1.0 / rv, dinv = -drv * inv * inv;
-      const int dst = j == 0 ? B_IA : j == 1 ? B_ITAU : B_IH;
-      W.B[q][dst] = inv; W.dB[q][dst] = dinv;
-    }
-    __syncwarp();
-    if (lane < nt) {
+    } else if (lane < nt) {  // role 3: constants of the mode and 1/τ
       const int q = lane;
-      const double ia = W.B[q][B_IA], dia = W.dB[q][B_IA];
       double* Bq = W.B[q]; double* dBq = W.dB[q];
-      Bq[B_ONE] = 1; Bq[B_K] = mk.k; Bq[B_K2] = mk.k2; Bq[B_IK] = mk.ik; Bq[B_IK2] = mk.ik2;
-      Bq[B_KD] = W.hv[q][2]; Bq[B_H] = W.hv[q][1]; Bq[B_CS2] = W.hv[q][3]; Bq[B_IA2] = ia * ia; Bq[B_R] = cd->R0 * ia;
-      dBq[B_ONE] = 0; dBq[B_K] = 0; dBq[B_K2] = 0; dBq[B_IK] = 0; dBq[B_IK2] = 0;
-      dBq[B_KD] = source ? W.hv[q][5] : W.hd[q][2]; dBq[B_H] = W.hd[q][1]; dBq[B_CS2] = W.hd[q][3];
-      dBq[B_IA2] = 2 * ia * dia; dBq[B_R] = cd->R0 * dia;
-      if (source) { W.src[0] = W.hv[q][4]; W.src[1] = W.hv[q][5]; W.src[2] = W.hv[q][6]; }
+      const double it = 1.0 / taus[q];
+      Bq[B_ONE] = 1; Bq[B_K] = mk.k; Bq[B_K2] = mk.k2; Bq[B_IK] = mk.ik; Bq[B_IK2] = mk.ik2; Bq[B_ITAU] = it;
+      dBq[B_ONE] = 0; dBq[B_K] = 0; dBq[B_K2] = 0; dBq[B_IK] = 0; dBq[B_IK2] = 0; dBq[B_ITAU] = -it * it;
     }
   }
   g.sync();
@@ -301,9 +322,12 @@ __device__ __forceinline__ void matvec(const Grp<NW>& g, const double* x, const 
                                        double* psi_out = nullptr) {
   const int gt = g.gt;
   const double* cv = C.cv;
-  double psi, rho;
-  functionals(g.fc, x, C.w, psi, rho);
-  const double phd = phidot(cv, rho, x[0], psi);
+  double psi = 0, phd = 0;
+  if (g.pp || phid_out || psi_out) {  // warp-uniform: only warps with metric-coupled rows need Ψ, Φ̇
+    double rho;
+    functionals(g.fc, x, C.w, psi, rho);
+    phd = phidot(cv, rho, x[0], psi);
+  }
   if (phid_out) *phid_out = phd;
   if (psi_out) *psi_out = psi;
   const double k34 = 0.75 * k;
@@ -326,12 +350,15 @@ template <int NW, int NSL>
 __device__ __forceinline__ void matvec_dtau(const Grp<NW>& g, const double* x, const CSet& C, const CompDesc* __restrict__ comps,
                                             const ModelDesc& M, double k, double (&out)[NSL], double* dpsi_out = nullptr) {
   const int gt = g.gt;
-  double psi, rho, dpsi, drho;
-  functionals(g.fc, x, C.w, psi, rho);
-  functionals(g.fc, x, C.wd, dpsi, drho);
+  double psi = 0, dpsi = 0, phd = 0, dphd = 0;
   const double* cv = C.cv; const double* cvd = C.cvd;
-  const double phd = phidot(cv, rho, x[0], psi);
-  const double dphd = cvd[CV_PA] * rho + cv[CV_PA] * drho + cvd[CV_PB] * x[0] + cvd[CV_MH] * psi + cv[CV_MH] * dpsi;
+  if (g.pp || dpsi_out) {  // warp-uniform, as in matvec
+    double rho, drho;
+    functionals(g.fc, x, C.w, psi, rho);
+    functionals(g.fc, x, C.wd, dpsi, drho);
+    phd = phidot(cv, rho, x[0], psi);
+    dphd = cvd[CV_PA] * rho + cv[CV_PA] * drho + cvd[CV_PB] * x[0] + cvd[CV_MH] * psi + cv[CV_MH] * dpsi;
+  }
   if (dpsi_out) *dpsi_out = dpsi;
   const double k34 = 0.75 * k;
 #pragma unroll
