@@ -217,7 +217,11 @@ def run_ours(args):
                 "h2d_bytes_per_step": int(8 * (3 * NK + 2 * NTAU + 2 * len(ls))), "d2h_bytes_per_step": int(8 * 3 * len(ls) + 4 * NK)},
         "phases_ms": {k: round(float(np.mean([p[k] for p in phases])), 3) for k in phases[0]},
         "roofline": {"bound": "fp64", "achieved": round(achieved, 5), "peak": round(fp64_peak, 3), "unit": "TFLOP/s",
-                     "frac": round(achieved / fp64_peak, 5), "traffic": None,
+                     "frac": round(achieved / fp64_peak, 5),
+                     # dram__bytes_read.sum + dram__bytes_write.sum of one full pt_kernel launch of this
+                     # workload (ncu, profiles/launches_bench_lcdm_massive_nu.md): 1.98 MB + 2.66 MB; the
+                     # coefficient tables stay in L1/L2, the kernel is FP64-latency bound
+                     "traffic": 4.64e6,
                      "kernel": "pt_kernel (perturbation modes)", "flops_per_step": fl, "steps_per_launch": steps_total,
                      "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 entry in MEASURED_PEAKS.json)"},
         "accuracy": accuracy,

@@ -338,8 +338,8 @@ __device__ __forceinline__ void matvec(const Grp<NW>& g, const double* x, const 
     if (i < M.n) {
       const CompDesc& D = comps[i];
       o = cv[D.sp] * (D.A * x[D.ip] + D.C * x[D.inx]) + (cv[D.dg] + cv[D.tr]) * x[i];
-      if ((g.pp >> s) & 1u) o += cv[D.phid] * phd + cv[D.psid] * psi;
       if (s == 0 && gt < 32) o += cv[D.e0] * x[D.e0c] + cv[D.e1] * x[D.e1c] + cv[D.e2] * x[D.e2c] + cv[D.dx] * (x[D.dxa] - k34 * x[D.dxb]);
+      if ((g.pp >> s) & 1u) o += cv[D.phid] * phd + cv[D.psid] * psi;
     }
     out[s] = o;
   }
@@ -754,7 +754,7 @@ __device__ __forceinline__ void stage_solve(const Grp<NW>& g, ModeMem<NW, NSL, S
 #pragma unroll
     for (int sl = 0; sl < NSL; ++sl) {
       const int i = comp_of<NW>(gt, sl);
-      if (i < M.n) W.r[i] = (ST)(b[sl] - (s * U[sl] - JU[sl]));
+      if (i < M.n) W.r[i] = (ST)(b[sl] - (s * U[sl] - JU[sl]));  // s U - J U ≈ b first: rounding of order ε|b|, not ε|J U|
     }
     g.sync();
     solve_W(g, W, F, M, scan);
@@ -1043,7 +1043,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         g.sync();
         matvec<NW, NSL>(g, W.x, W.cs[s2], comps, M, k, Fv);
 #pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C21 * U1[sl]) + h * rw::d2 * ft[sl];
+        for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + (ih * (rw::C21 * U1[sl]) + h * rw::d2 * ft[sl]);
         stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U2);
         // stage 3
 #pragma unroll
@@ -1051,7 +1051,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         g.sync();
         matvec<NW, NSL>(g, W.x, W.cs[s3], comps, M, k, Fv);
 #pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C31 * U1[sl] + rw::C32 * U2[sl]) + h * rw::d3 * ft[sl];
+        for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + (ih * (rw::C31 * U1[sl] + rw::C32 * U2[sl]) + h * rw::d3 * ft[sl]);
         stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U3);
         // stage 4
 #pragma unroll
@@ -1059,7 +1059,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         g.sync();
         matvec<NW, NSL>(g, W.x, W.cs[s4], comps, M, k, Fv);
 #pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C41 * U1[sl] + rw::C42 * U2[sl] + rw::C43 * U3[sl]) + h * rw::d4 * ft[sl];
+        for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + (ih * (rw::C41 * U1[sl] + rw::C42 * U2[sl] + rw::C43 * U3[sl]) + h * rw::d4 * ft[sl]);
         stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U4);
         // stage 5 (at t + h)
         double Y[NSL];
