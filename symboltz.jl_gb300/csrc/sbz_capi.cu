@@ -146,7 +146,7 @@ void sbz_default_opts(sbz_opts* o) {
   o->bg_rtol = 1e-7; o->bg_atol = 1e-7; o->pt_rtol = 1e-5; o->pt_atol = 1e-5;
   o->tau_ini = 1e-6; o->tau_max = 100.0; o->maxiters = 100000;
   o->precision = SBZ_MIXED; o->refine_iters = 3; o->table_points = 8192; o->warps_per_block = 0; o->warps_per_mode = 0; o->blocks_per_sm = 0;
-  o->los_precision = -1; o->refine_skip = 1e-5;
+  o->los_precision = -1; o->refine_skip = -1.0;
 }
 
 const char* sbz_last_error(void) { return g_err.c_str(); }

@@ -21,8 +21,13 @@ int pt_launch(const PtArgs& A, int precision, int warps_per_block, int warps_per
   // four-warp groups: two resident per SM, so the slowest modes share an SM's FP64 pipes with at
   // most one other mode (measured on a 1000-mode spectrum: 0.57 s against 0.70 s at full occupancy)
   if (blocks_per_sm <= 0 && nw == 4) blocks_per_sm = 2;
-  if (precision == SBZ_MIXED)
-    return nw == 1 ? pt_launch_f32_w1(A, nw, warps_per_block, blocks_per_sm, num_sms, stream) : pt_launch_f32_w2_w4(A, nw, warps_per_block, blocks_per_sm, num_sms, stream);
+  if (precision == SBZ_MIXED) {
+    // lazy refinement left open: on for four-warp groups (latency-bound: fewer dependent phases
+    // per step), off for narrower ones (throughput-bound batches measured 11 % slower with it)
+    PtArgs B = A;
+    if (B.refine_skip < 0) B.refine_skip = nw == 4 ? 1e-5f : 0.0f;
+    return nw == 1 ? pt_launch_f32_w1(B, nw, warps_per_block, blocks_per_sm, num_sms, stream) : pt_launch_f32_w2_w4(B, nw, warps_per_block, blocks_per_sm, num_sms, stream);
+  }
   return nw == 1 ? pt_launch_f64_w1(A, nw, warps_per_block, blocks_per_sm, num_sms, stream) : pt_launch_f64_w2_w4(A, nw, warps_per_block, blocks_per_sm, num_sms, stream);
 }
 

@@ -28,7 +28,7 @@ struct PtArgs {
   double rtol, atol;
   int64_t maxiters;
   int refine;
-  float refine_skip;          // skip stages 2-6 refinement below this stage-1 correction (0: never)
+  float refine_skip;          // skip stages 2-6 refinement below this stage-1 correction (0: never; < 0: by launch shape)
   unsigned int* counter;      // device work-queue counter, zero before launch
 };
 

@@ -212,66 +212,57 @@ __device__ __forceinline__ void table_hermite(const CosmoDesc* __restrict__ cd, 
 // τ-dependent coefficients at nt ≤ kMaxT times into sets cs[set[q]]; derivative sets where bit q
 // of dmask is set.  source = true (nt = 1): also fetch e^{-κ}, κ̈, κ⃛ and use the Taylor-mode κ̈
 // as dκ̇/dτ (the line-of-sight sources differentiate the background along its ODE,
-// src/models/cosmologies.jl:99-105).  The base scalars are formed by four independent roles that
-// run on different warps (folded onto fewer warps when NW < 4), each interpolating the table
-// itself: role 0/1 the seven table quantities of the times without/with derivatives, with 1/a and
-// 1/ℋ; role 2 the momentum-bin energies; role 3 the k constants and 1/τ.  The expressions are then
-// spread over the group.  The caller guarantees that no thread still reads the target sets; the
-// call ends with a group barrier.
+// src/models/cosmologies.jl:99-105).  Warp 0 forms the base scalars in one pass, lane = 8 q + c:
+// lane c < 7 interpolates table quantity c at time q once; lanes c = 0, 1, 7 then share one
+// reciprocal path (1/a, 1/ℋ, 1/τ) and lanes c < nx one momentum-bin energy path (a from lane 8q by
+// shuffle), so no quantity is interpolated twice.  The expressions are then spread over the group.
+// The caller guarantees that no thread still reads the target sets; the call ends with a group
+// barrier.
 template <int NW, int NSL, typename ST>
 __device__ __forceinline__ void coef_eval(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const int* set, const double* taus, int nt,
                           unsigned dmask, bool source, const CosmoDesc* cd, const double* __restrict__ tab,
                           int nexpr, int nx, const ModeK& mk) {
-  const int lane = g.lane;
-  for (int role = g.wq; role < 4; role += NW) {
-    if (role <= 1) {  // table quantities: lane = 8 q + quantity
-      const int q = lane >> 3, c = lane & 7;
-      if (q < nt && c < 7 && (int)((dmask >> q) & 1u) == role) {
-        const bool dq = role == 1;
-        double v, d;
-        table_hermite(cd, tab, taus[q], c, dq, v, d);
-        double* Bq = W.B[q]; double* dBq = W.dB[q];
-        if (c == 0) {  // a: 1/a, 1/a², R = R0/a
-          const double ia = 1.0 / v;
-          Bq[B_IA] = ia; Bq[B_IA2] = ia * ia; Bq[B_R] = cd->R0 * ia;
-          if (dq) { const double dia = -d * ia * ia; dBq[B_IA] = dia; dBq[B_IA2] = 2 * ia * dia; dBq[B_R] = cd->R0 * dia; }
-        } else if (c == 1) {  // ℋ and 1/ℋ
-          const double ih = 1.0 / v;
-          Bq[B_H] = v; Bq[B_IH] = ih;
-          if (dq) { dBq[B_H] = d; dBq[B_IH] = -d * ih * ih; }
-        } else if (c == 2) {  // κ̇
-          Bq[B_KD] = v;
-          if (dq && !source) dBq[B_KD] = d;
-        } else if (c == 3) {  // c_s²
-          Bq[B_CS2] = v;
-          if (dq) dBq[B_CS2] = d;
-        } else {  // e^{-κ}, κ̈, κ⃛: line-of-sight sources only (κ̈ is then dκ̇/dτ)
-          if (source) W.src[c - 4] = v;
-          if (source && c == 5) dBq[B_KD] = v;
-        }
+  if (g.wq == 0) {
+    const int lane = g.lane, q = lane >> 3, c = lane & 7;
+    const bool live = q < nt;
+    const bool dq = live && ((dmask >> q) & 1u);
+    double v = 0, d = 0;
+    if (live && c < 7) table_hermite(cd, tab, taus[q], c, dq, v, d);
+    const double a = __shfl_sync(FULL, v, lane & ~7), da = __shfl_sync(FULL, d, lane & ~7);
+    double* Bq = W.B[live ? q : 0]; double* dBq = W.dB[live ? q : 0];
+    if (live && (c <= 1 || c == 7)) {  // reciprocals of a, ℋ, τ
+      const double rv = c == 7 ? taus[q] : v, drv = c == 7 ? 1.0 : d;
+      const double inv = 1.0 / rv;
+      if (c == 0) {
+        Bq[B_IA] = inv; Bq[B_IA2] = inv * inv; Bq[B_R] = cd->R0 * inv;
+        if (dq) { const double dia = -drv * inv * inv; dBq[B_IA] = dia; dBq[B_IA2] = 2 * inv * dia; dBq[B_R] = cd->R0 * dia; }
+      } else if (c == 1) {
+        Bq[B_H] = v; Bq[B_IH] = inv;
+        if (dq) { dBq[B_H] = d; dBq[B_IH] = -drv * inv * inv; }
+      } else {
+        Bq[B_ITAU] = inv; Bq[B_ONE] = 1; Bq[B_K] = mk.k; Bq[B_K2] = mk.k2; Bq[B_IK] = mk.ik; Bq[B_IK2] = mk.ik2;
+        if (dq) { dBq[B_ITAU] = -inv * inv; dBq[B_ONE] = 0; dBq[B_K] = 0; dBq[B_K2] = 0; dBq[B_IK] = 0; dBq[B_IK2] = 0; }
       }
-    } else if (role == 2) {  // momentum-bin energies E_b = sqrt(x_b² + (y0 a)²): lane = 8 q + b
-      const int q = lane >> 3, b = lane & 7;
-      if (q < nt && b < nx) {
-        const bool dq = (dmask >> q) & 1u;
-        double a, da;
-        table_hermite(cd, tab, taus[q], 0, dq, a, da);
-        const double xj = cd->xq[b], y0a = cd->y0 * a;
-        const double E2 = xj * xj + y0a * y0a;
-        const double iE = rsqrt(E2), E = E2 * iE;
-        const double ixj = cd->ixq[b];
-        W.B[q][B_Q + b] = xj * iE; W.B[q][B_IQ + b] = E * ixj; W.B[q][B_E + b] = E; W.B[q][B_IE + b] = iE;
-        if (dq) {
-          const double dE = cd->y0 * y0a * da * iE;
-          W.dB[q][B_Q + b] = -xj * dE * iE * iE; W.dB[q][B_IQ + b] = dE * ixj; W.dB[q][B_E + b] = dE; W.dB[q][B_IE + b] = -dE * iE * iE;
-        }
+    } else if (live && c == 2) {  // κ̇ (for the sources, dκ̇/dτ is κ̈ from lane c = 5)
+      Bq[B_KD] = v;
+      if (dq && !source) dBq[B_KD] = d;
+    } else if (live && c == 3) {  // c_s²
+      Bq[B_CS2] = v;
+      if (dq) dBq[B_CS2] = d;
+    } else if (live && c < 7 && source) {  // e^{-κ}, κ̈, κ⃛
+      W.src[c - 4] = v;
+      if (c == 5) dBq[B_KD] = v;
+    }
+    if (live && c < nx) {  // momentum-bin energy E_c = sqrt(x_c² + (y0 a)²)
+      const double xj = cd->xq[c], y0a = cd->y0 * a;
+      const double E2 = xj * xj + y0a * y0a;
+      const double iE = rsqrt(E2), E = E2 * iE;
+      const double ixj = cd->ixq[c];
+      Bq[B_Q + c] = xj * iE; Bq[B_IQ + c] = E * ixj; Bq[B_E + c] = E; Bq[B_IE + c] = iE;
+      if (dq) {
+        const double dE = cd->y0 * y0a * da * iE;
+        dBq[B_Q + c] = -xj * dE * iE * iE; dBq[B_IQ + c] = dE * ixj; dBq[B_E + c] = dE; dBq[B_IE + c] = -dE * iE * iE;
       }
-    } else if (lane < nt) {  // role 3: constants of the mode and 1/τ
-      const int q = lane;
-      double* Bq = W.B[q]; double* dBq = W.dB[q];
-      const double it = 1.0 / taus[q];
-      Bq[B_ONE] = 1; Bq[B_K] = mk.k; Bq[B_K2] = mk.k2; Bq[B_IK] = mk.ik; Bq[B_IK2] = mk.ik2; Bq[B_ITAU] = it;
-      dBq[B_ONE] = 0; dBq[B_K] = 0; dBq[B_K2] = 0; dBq[B_IK] = 0; dBq[B_IK2] = 0; dBq[B_ITAU] = -it * it;
     }
   }
   g.sync();
@@ -1212,8 +1203,11 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
   }
 }
 
+// Register budget: four-warp groups run at most two per SM (tail-bound spectra), so they may use up
+// to 256 registers per thread and need not spill; narrower groups keep three 128-thread blocks per
+// SM (throughput-bound batches), accepting a few spilled registers for the occupancy.
 template <int NW, int NSL, typename ST>
-__global__ void __launch_bounds__(128) pt_kernel(PtArgs A) {
+__global__ void __launch_bounds__(128, NW >= 4 ? 2 : 3) pt_kernel(PtArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ModelDesc& M = *reinterpret_cast<ModelDesc*>(smem_raw);
   CompDesc* comps = reinterpret_cast<CompDesc*>(smem_raw + ((sizeof(ModelDesc) + 15) & ~size_t(15)));

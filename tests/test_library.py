@@ -36,7 +36,7 @@ def test_default_options():
         pytest.skip("library not built")
     o = _lib.Opts()
     _lib.lib().sbz_default_opts(C.byref(o))
-    assert o.bg_rtol == 1e-7 and o.pt_rtol == 1e-5 and o.tau_ini == 1e-6 and o.maxiters == 100000 and o.refine_iters == 3 and o.refine_skip == 1e-5
+    assert o.bg_rtol == 1e-7 and o.pt_rtol == 1e-5 and o.tau_ini == 1e-6 and o.maxiters == 100000 and o.refine_iters == 3 and o.refine_skip == -1.0
     assert o.precision == _lib.SBZ_MIXED
 
 
