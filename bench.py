@@ -20,6 +20,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -158,7 +159,7 @@ def run_ours(args):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     dev_ms, e2e_ms, pt_ms, phases = [], [], [], []
     steps_total = 0
-    with Clocks(os.path.join(ROOT, "gpurun_out", "clocks_bench.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/clocks_bench.csv") as ck:
+    with Clocks(args.clocks_log) as ck:
         for _ in range(args.steps):
             flush.fill_(1.0)
             torch.cuda.synchronize()
@@ -350,7 +351,7 @@ def run_batched(args):
 def run_surrogate(args):
     """Learned part: training data from the GPU solver (scrambled-Sobol box points; perturbation
     factors on 400 k × 500 τ), training with the library's BF16 tcgen05 kernels, then C_l (D_l, TT/TE/EE
-    to l = 2500) of held-out cosmologies through surrogate + solver fallback, judged against the
+    to l = 2500) of held-out cosmologies through surrogate + solver fallback, compared with the
     all-FP64 solver; cosmologies/s of that path against the plain (mixed-precision) solver path."""
     import torch
     import symboltz as S
@@ -378,27 +379,27 @@ def run_surrogate(args):
     jl = S.SphericalBesselCache(ls)
     kin = S.CubicSplineInterpolator(ks, f=np.log)
     lall = np.arange(2, LMAX + 1)
-    # judge: all-FP64 solver on the same grids
+    # accuracy reference: the all-FP64 solver on the same grids
     _, taus, _, _ = sur.solve_factors(test[:1])
-    judge, t_solver = [], 0.0
+    ref64, t_solver = [], 0.0
     for th in test:
         p64 = S.CosmologyProblem(M, SG.box_params(th), precision="fp64")
         bg = p64.solvebg()
         tt = SG.cmb_taus(bg.t(0), bg.tau0[0], sur.ntau)
-        judge.append(S.spectrum_cmb(["TT", "TE", "EE"], p64, jl, lall, kinterp=kin, taus=tt, normalization="Dl"))
+        ref64.append(S.spectrum_cmb(["TT", "TE", "EE"], p64, jl, lall, kinterp=kin, taus=tt, normalization="Dl"))
         pm = S.CosmologyProblem(M, SG.box_params(th))
         t1 = time.perf_counter()
         bgm = pm.solvebg()
         S.spectrum_cmb(["TT", "TE", "EE"], pm, jl, lall, kinterp=kin, taus=SG.cmb_taus(bgm.t(0), bgm.tau0[0], sur.ntau), normalization="Dl")
         t_solver += time.perf_counter() - t1
-    judge = np.stack(judge)
+    ref64 = np.stack(ref64)
     t1 = time.perf_counter()
     Dl, errs, fb = sur.spectra(test, jl, lall, kin, tol=args.surrogate_tol)
     t_sur = time.perf_counter() - t1
-    den = [np.abs(judge[..., 0]), np.sqrt(np.abs(judge[..., 0] * judge[..., 2])), np.abs(judge[..., 2])]
-    rel = np.stack([np.max(np.abs(Dl[..., i] - judge[..., i]) / den[i], axis=1) for i in range(3)], axis=1)  # [cosmo][mode]
+    den = [np.abs(ref64[..., 0]), np.sqrt(np.abs(ref64[..., 0] * ref64[..., 2])), np.abs(ref64[..., 2])]
+    rel = np.stack([np.max(np.abs(Dl[..., i] - ref64[..., i]) / den[i], axis=1) for i in range(3)], axis=1)  # [cosmo][mode]
     Dl_raw, _, _ = sur.spectra(test, jl, lall, kin, fallback=False)
-    rel_raw = np.stack([np.max(np.abs(Dl_raw[..., i] - judge[..., i]) / den[i], axis=1) for i in range(3)], axis=1)
+    rel_raw = np.stack([np.max(np.abs(Dl_raw[..., i] - ref64[..., i]) / den[i], axis=1) for i in range(3)], axis=1)
     n = len(test)
     line = {"metric": "cosmologies/s (surrogate + fallback vs solver)", "value": round(n / t_sur, 3), "unit": "cosmologies/s",
             "workload": f"{n} held-out cosmologies from the box, C_l TT/TE/EE to l={LMAX} (D_l), 400 k x 500 tau",
@@ -465,6 +466,8 @@ def main():
     ap.add_argument("--train-seconds", type=float, default=120.0)
     ap.add_argument("--test-cosmologies", type=int, default=16)
     ap.add_argument("--surrogate-tol", type=float, default=1e-3)
+    ap.add_argument("--clocks-log", default=os.path.join(tempfile.gettempdir(), "sbz_bench_clocks.csv"),
+                    help="CSV of the nvidia-smi clock samples taken during the timed region")
     ap.add_argument("--workload", choices=("spectrum", "batched", "surrogate"), default="spectrum",
                     help="spectrum: the headline single-cosmology C_l workload; batched: 256 cosmologies, ragged k grids")
     ap.add_argument("--profile-case", choices=("pt", "los", "mlp"), default=None,

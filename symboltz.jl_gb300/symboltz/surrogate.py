@@ -9,8 +9,8 @@ Its sources go through the regular k-interpolation → line-of-sight → C_ℓ p
 (``sbz_spectrum_cmb_sources``).  Each cosmology gets an error estimate in the C_ℓ metric: 48 probe
 modes are also solved with the real solver, and D_ℓ from the surrogate's and the solver's sources
 at those modes (same pipeline, same probe grid) are compared; a cosmology whose estimate exceeds
-the tolerance is recomputed with the solver (fallback), which therefore remains the judge of every
-result.
+the tolerance is recomputed with the solver (fallback), which therefore remains the reference for
+every result.
 """
 import ctypes as C
 
