@@ -291,3 +291,38 @@ def test_set_params_reuses_the_problem(S):
     for i in range(3):
         one, _, _ = S.solvept(S.CosmologyProblem(M, sets[1 + i], warps_per_mode=2), ks, ti, output="delta_m")
         np.testing.assert_array_equal(got[cos == i], one)
+
+
+# plain ΛCDM: h = 0.67, ω_c = 0.12, ω_b = 0.022, T_CMB = 2.7255 K, N_eff = 3.046 massless ν,
+# Y_He = 0.245, ln(1e10 A_s) = 3.04, n_s = 0.965; photon and massless-ν hierarchies to l = 10
+PLAIN_PARAMS = dict(h=0.67, Omega_c=0.12 / 0.67**2, Omega_b=0.022 / 0.67**2, T0=2.7255, Neff=3.046, YHe=0.245, ln_As1e10=3.04,
+                    ns=0.965, m_nu_eV=0.0, N_nu=0.0)
+MODEL10_MASSLESS = dict(lmax_g=10, lmax_nu=10, lmax_h=10, nx=0, Hswitch=1, Heswitch=6, reionization=1)
+
+
+def test_plain_lcdm_fp64_rtol1e6(S):
+    """Plain ΛCDM in FP64 at rtol = atol = 1e-6: 100 modes log-spaced over 1e-4..1 h/Mpc, P(k) at
+    z = 0 and the line-of-sight sources on 500 times, against the oracle at the same tolerance; the
+    mixed-precision solver's P(k) on the same modes at the same bar."""
+    M = S.ΛCDM(lmax=10, massive_nu=False)
+    prob = S.CosmologyProblem(M, PLAIN_PARAMS, pt_rtol=1e-6, pt_atol=1e-6, precision="fp64")
+    bgo = O.Background(PLAIN_PARAMS, MODEL10_MASSLESS, pt_rtol=1e-6, pt_atol=1e-6)
+    assert prob.nstate == bgo.nstate == 38
+    khm = S.loggrid(1e-4, 1.0, length=100)
+    ks = S.k_from_hMpc(khm)
+    P, st = S.spectrum_matter(prob, ks, return_status=True)
+    Po, sto, _ = O.spectrum_matter(bgo, ks)
+    assert np.all(st == 0) and np.all(sto == 0)
+    rel = np.abs(P / Po - 1)
+    assert np.max(rel[khm > 0.15]) < 1e-4, np.max(rel)
+    assert np.linalg.norm(P - Po) <= 1e-4 * np.linalg.norm(Po)
+    mixed = S.CosmologyProblem(M, PLAIN_PARAMS, pt_rtol=1e-6, pt_atol=1e-6)
+    Pm, stm = S.spectrum_matter(mixed, ks, return_status=True)
+    assert np.all(stm == 0) and np.linalg.norm(Pm - Po) <= 1e-4 * np.linalg.norm(Po)
+    taus = np.linspace(bgo.tau0 * 0.01, bgo.tau0 * 0.999, 500)
+    out, st, _ = S.solvept(prob, ks, 1e-6, saveat=taus, output="sources")
+    ref, sto, _ = bgo.solve_pt(ks, 1e-6, taus, mode=0)
+    assert np.all(st == 0) and np.all(sto == 0)
+    for s in range(3):
+        scale = np.max(np.abs(ref[:, :, s]), axis=1, keepdims=True) + 1e-300
+        assert np.max(np.abs(out[:, :, s] - ref[:, :, s]) / scale) < 1e-3, s
