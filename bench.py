@@ -224,7 +224,10 @@ def run_ours(args):
                      # coefficient tables stay in L1/L2, the kernel is FP64-latency bound
                      "traffic": 4.64e6,
                      "kernel": "pt_kernel (perturbation modes)", "flops_per_step": fl, "steps_per_launch": steps_total,
-                     "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 entry in MEASURED_PEAKS.json)"},
+                     "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 entry in MEASURED_PEAKS.json)",
+                     # the same launch against the HBM roofline: measured traffic over its CUDA-event time
+                     "hbm": {"achieved_gbs": round(4.64e6 / pt_avg / 1e9, 6), "peak_gbs": peaks.get("hbm_gbs"),
+                             "frac": round(4.64e6 / pt_avg / 1e9 / peaks["hbm_gbs"], 8) if peaks.get("hbm_gbs") else None}},
         "accuracy": accuracy,
         "gpu_launches": int(K * 6),
         "clocks": ck.summary(),
@@ -348,6 +351,22 @@ def run_batched(args):
     print(json.dumps(line), flush=True)
 
 
+def mlp_step_bytes(batch=65536, nin_pad=64, width=512, nhidden=4, nout_pad=64, nparams=794631):
+    """Algorithmic HBM bytes of one training step of the surrogate (each array read or written once
+    per kernel that touches it): forward layers read X_{l-1} and write X_l, Z_l and X_lᵀ (BF16), the
+    output layer writes FP32 Y; the loss reads Y and writes dY, dYᵀ; each backward dX GEMM reads its
+    output gradient and Z and writes dZ, dZᵀ; each weight-gradient GEMM reads dZᵀ and Xᵀ; Adam reads
+    and writes p, m, v and reads the gradient (FP32) and writes two BF16 copies of the weights."""
+    a, w = 2 * batch, width
+    fwd = a * nin_pad + 3 * a * w + (nhidden - 1) * (a * w + 3 * a * w) + a * w + 4 * batch * nout_pad
+    loss = 4 * batch * nout_pad + 2 * a * nout_pad
+    dx = (a * nout_pad + a * w + 2 * a * w) + (nhidden - 1) * (a * w + a * w + 2 * a * w)
+    dw = (a * w + a * nout_pad) + (nhidden - 1) * (2 * a * w) + (a * w + a * nin_pad)
+    adam = nparams * (7 * 4 + 2 * 2)
+    gather = batch * (8 * 4 + 7 * 4) + 2 * a * nin_pad
+    return fwd + loss + dx + dw + adam + gather
+
+
 def run_surrogate(args):
     """Learned part: training data from the GPU solver (scrambled-Sobol box points; perturbation
     factors on 400 k × 500 τ), training with the library's BF16 tcgen05 kernels, then C_l (D_l, TT/TE/EE
@@ -416,6 +435,15 @@ def run_surrogate(args):
                          "tflops": round(steps * flops_step / t_train / 1e12, 1), "batch": 65536,
                          "loss_first_last": [losses[0], losses[-1]], "mse_train_standardised": mse_train},
             "model": "MLP 8 -> 4x512 SiLU -> 7 (perturbation factors), BF16 tcgen05 GEMMs, FP32 accumulate, Adam"}
+    peaks = measured_peaks()
+    step_s = t_train / steps
+    nbytes = mlp_step_bytes()
+    line["training"]["roofline"] = {
+        "bound": "hbm", "unit": "GB/s", "achieved": round(nbytes / step_s / 1e9, 1), "peak": peaks.get("hbm_gbs"),
+        "frac": round(nbytes / step_s / 1e9 / peaks["hbm_gbs"], 4) if peaks.get("hbm_gbs") else None, "traffic": None,
+        "bytes_per_step": nbytes, "ms_per_step": round(step_s * 1e3, 4),
+        "tensor_tflops": round(steps * flops_step / t_train / 1e12, 1), "tensor_peak_sustained": peaks.get("bf16_tflops_sustained"),
+        "tensor_frac": round(steps * flops_step / t_train / 1e12 / peaks["bf16_tflops_sustained"], 4) if peaks.get("bf16_tflops_sustained") else None}
     print(json.dumps(line), flush=True)
 
 
