@@ -417,7 +417,9 @@ def run_surrogate(args):
     t_sur = time.perf_counter() - t1
     den = [np.abs(ref64[..., 0]), np.sqrt(np.abs(ref64[..., 0] * ref64[..., 2])), np.abs(ref64[..., 2])]
     rel = np.stack([np.max(np.abs(Dl[..., i] - ref64[..., i]) / den[i], axis=1) for i in range(3)], axis=1)  # [cosmo][mode]
+    t1 = time.perf_counter()
     Dl_raw, _, _ = sur.spectra(test, jl, lall, kin, fallback=False)
+    t_raw = time.perf_counter() - t1
     rel_raw = np.stack([np.max(np.abs(Dl_raw[..., i] - ref64[..., i]) / den[i], axis=1) for i in range(3)], axis=1)
     n = len(test)
     line = {"metric": "cosmologies/s (surrogate + fallback vs solver)", "value": round(n / t_sur, 3), "unit": "cosmologies/s",
@@ -429,6 +431,9 @@ def run_surrogate(args):
                                    "surrogate_only": {"median": float(np.median(rel_raw.max(axis=1))), "max": float(rel_raw.max()),
                                                       "median_by_spectrum": dict(zip(("TT", "TE", "EE"),
                                                                                      np.median(rel_raw, axis=0).round(6).tolist()))}},
+            "surrogate_only": {"cosmologies_per_s": round(n / t_raw, 3), "speedup_vs_solver": round(t_solver / t_raw, 2),
+                               "cl_max_rel_median": float(np.median(rel_raw.max(axis=1))),
+                               "note": "backgrounds + network + line of sight, no mode solved: what the network gains in speed, at its accuracy"},
             "estimate_vs_true_surrogate_error": [[round(float(e), 6), round(float(t), 6)] for e, t in zip(errs, rel_raw.max(axis=1))],
             "training": {"cosmologies": args.train_cosmologies, "samples": int(args.train_cosmologies * len(ks) * sur.ntau),
                          "data_s": round(t_data, 2), "steps": steps, "train_s": round(t_train, 2),

@@ -192,6 +192,18 @@ class SourceSurrogate:
         vis = np.stack([self.visibility(bg.coefficients(taus[c], c)) for c in range(len(thetas))])
         return out.reshape(len(thetas), nk, self.ntau, 7), taus, vis, prob
 
+    def backgrounds(self, thetas):
+        """Times [ncos][ntau], visibilities [ncos][4][ntau] and the problem of the given parameter
+        points from their backgrounds alone (no perturbation modes solved)."""
+        from . import CosmologyProblem
+        prob = CosmologyProblem(self.M, [box_params(t) for t in thetas])
+        bg = prob.solvebg()
+        if np.any(bg.status != 0):
+            raise L.SbzError("background failed for a cosmology of the box")
+        taus = np.stack([cmb_taus(bg.t(c), bg.tau0[c], self.ntau) for c in range(len(thetas))])
+        vis = np.stack([self.visibility(bg.coefficients(taus[c], c)) for c in range(len(thetas))])
+        return taus, vis, prob
+
     def weights(self, vis):
         """Per-time multipliers of the learned factors: the visibility envelope for f0, f2..f6 and
         e^{-κ} for the ISW factor f1."""
@@ -310,12 +322,18 @@ class SourceSurrogate:
     def spectra(self, thetas, jl, ls_out, kinterp, modes=("TT", "TE", "EE"), tol=1e-3, kprobe=None, fallback=True):
         """C_ℓ (D_ℓ) for each θ: surrogate sources through the line-of-sight pipeline, or the solver
         for cosmologies whose held-out error estimate (probe_error, relative D_ℓ) exceeds tol.
-        Returns (Dl [ncos][nl][nmodes], error estimates, fallback mask)."""
+        fallback=False: the surrogate alone (no probe modes, error estimates NaN).  Returns
+        (Dl [ncos][nl][nmodes], error estimates, fallback mask)."""
         from . import CosmologyProblem, spectrum_cmb
-        kprobe = self.probe_kgrid() if kprobe is None else np.asarray(kprobe)
-        Fp, taus, vis, prob = self.solve_factors(thetas, ks=kprobe)
-        errs = np.array([self.probe_error(t, taus[c], vis[c], Fp[c], kprobe, prob, c, jl, ls_out) for c, t in enumerate(thetas)])
-        fb = (errs > tol) if fallback else np.zeros(len(thetas), dtype=bool)
+        if fallback:
+            kprobe = self.probe_kgrid() if kprobe is None else np.asarray(kprobe)
+            Fp, taus, vis, prob = self.solve_factors(thetas, ks=kprobe)
+            errs = np.array([self.probe_error(t, taus[c], vis[c], Fp[c], kprobe, prob, c, jl, ls_out) for c, t in enumerate(thetas)])
+            fb = errs > tol
+        else:  # surrogate only: backgrounds, network, line of sight; no mode is solved
+            taus, vis, prob = self.backgrounds(thetas)
+            errs = np.full(len(thetas), np.nan)
+            fb = np.zeros(len(thetas), dtype=bool)
         out = []
         for c, t in enumerate(thetas):
             if fb[c]:

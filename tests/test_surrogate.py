@@ -92,6 +92,9 @@ def test_surrogate_sources_through_the_line_of_sight_with_fallback():
     ls = np.arange(2, 393)
     Dl, err, fb = sur.spectra(test, jl, ls, kin, tol=np.inf)
     assert not fb.any() and np.all(np.isfinite(Dl)) and np.all(np.isfinite(err))
+    Draw, err_raw, fb_raw = sur.spectra(test, jl, ls, kin, fallback=False)  # no probe modes solved
+    assert not fb_raw.any() and np.all(np.isnan(err_raw))
+    np.testing.assert_allclose(Draw, Dl, rtol=1e-12)
     Dfb, err2, fb2 = sur.spectra(test, jl, ls, kin, tol=0.0)
     assert fb2.all()
     np.testing.assert_allclose(err2, err)
