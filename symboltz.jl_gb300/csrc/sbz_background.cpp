@@ -358,21 +358,7 @@ int background_solve(Background& B, const sbz_params& p, const sbz_model& m, con
 
 // Hermite spline of the unknowns; S = double (value) or Tay<1> (value and d/dτ)
 template <class S>
-static void spline_at(const Background& B, double tau, S* y) {
-  const auto& K = B.knots;
-  int lo = 0, hi = (int)K.size() - 1;
-  if (tau <= K[0].t) hi = 1;
-  else if (tau >= K[hi].t) lo = hi - 1;
-  else while (hi - lo > 1) { const int mid = (lo + hi) >> 1; (K[mid].t <= tau ? lo : hi) = mid; }
-  const BgKnot &A = K[lo], &Bk = K[lo + 1];
-  const double h = Bk.t - A.t, s = (tau - A.t) / h, s2 = s * s, s3 = s2 * s;
-  const double h00 = 2 * s3 - 3 * s2 + 1, h10 = s3 - 2 * s2 + s, h01 = -2 * s3 + 3 * s2, h11 = s3 - s2;
-  const double g00 = (6 * s2 - 6 * s) / h, g10 = 3 * s2 - 4 * s + 1, g01 = (6 * s - 6 * s2) / h, g11 = 3 * s2 - 2 * s;
-  for (int j = 0; j < NB; ++j) {
-    y[j] = S(h00 * A.y[j] + h10 * h * A.s[j] + h01 * Bk.y[j] + h11 * h * Bk.s[j]);
-    if constexpr (!std::is_same<S, double>::value) y[j].c[1] = g00 * A.y[j] + g10 * A.s[j] + g01 * Bk.y[j] + g11 * Bk.s[j];
-  }
-}
+static void spline_at(const Background& B, double tau, S* y) { knots_spline<S>(B.knots.data(), (int)B.knots.size(), tau, y); }
 
 void background_spline(const Background& B, double tau, double* y) { spline_at<double>(B, tau, y); }
 
@@ -398,44 +384,22 @@ void background_eval(const Background& B, double tau, double* out) {
 }
 
 // Coefficient table on ln τ nodes (see kTabStride)
-void background_table(Background& B, int ntab) {
+void background_table_grid(Background& B, int ntab) {
   B.ntab = ntab;
   B.lnt0 = std::log(B.tau_start);
   B.dlnt = (std::log(B.tau0) - B.lnt0) / (ntab - 1);
-  B.tab.assign((size_t)ntab * kTabStride, 0.0);
+  B.tab.clear();
   B.tabtau.resize(ntab);
+  for (int g = 0; g < ntab; ++g)
+    B.tabtau[g] = (g == ntab - 1) ? B.tau0 : (g == 0 ? B.tau_start : std::exp(B.lnt0 + g * B.dlnt));
+}
+
+void background_table_values(Background& B) {
+  const int ntab = B.ntab;
+  B.tab.assign((size_t)ntab * kTabStride, 0.0);
   // nodes are independent; inside an outer parallel loop over cosmologies this runs serially
 #pragma omp parallel for schedule(static)
-  for (int g = 0; g < ntab; ++g) {
-    double tau = (g == ntab - 1) ? B.tau0 : (g == 0 ? B.tau_start : std::exp(B.lnt0 + g * B.dlnt));
-    B.tabtau[g] = tau;
-    double* T = &B.tab[(size_t)g * kTabStride];
-    {  // chain rule through the spline: pt right-hand-side coefficients
-      Tay<1> y[NB], f[NB];
-      spline_at<Tay<1>>(B, tau, y);
-      BgState<Tay<1>> st;
-      background_rhs<Tay<1>>(B.P, y, f, &st);
-      T[0] = st.a.c[0]; T[1] = st.a.c[1];
-      T[2] = st.Hc.c[0]; T[3] = st.Hc.c[1];
-      T[4] = st.kd.c[0]; T[5] = st.kd.c[1];
-      T[6] = st.cs2.c[0]; T[7] = st.cs2.c[1];
-    }
-    {  // Taylor mode through the splined state: visibility derivatives for the sources
-      constexpr int N = 4;
-      double yv[NB]; background_spline(B, tau, yv);
-      Tay<N> z[NB], g[NB];
-      for (int j = 0; j < NB; ++j) z[j] = Tay<N>(yv[j]);
-      for (int ord = 0; ord < N; ++ord) {
-        background_rhs<Tay<N>>(B.P, z, g, nullptr);
-        for (int j = 0; j < NB; ++j) z[j].c[ord + 1] = g[j].c[ord] / (ord + 1);
-      }
-      background_rhs<Tay<N>>(B.P, z, g, nullptr);
-      const Tay<N> ek = exp(-(z[1] - B.kappa0));
-      T[8] = ek.c[0]; T[9] = ek.c[1];
-      T[10] = g[1].c[1]; T[11] = 2 * g[1].c[2];
-      T[12] = 2 * g[1].c[2]; T[13] = 6 * g[1].c[3];
-    }
-  }
+  for (int g = 0; g < ntab; ++g) table_node(B.P, B.knots.data(), (int)B.knots.size(), B.kappa0, B.tabtau[g], &B.tab[(size_t)g * kTabStride]);
 }
 
 void table_eval(const Background& B, double tau, double* out) {

@@ -4,15 +4,14 @@
 #pragma once
 #include <vector>
 #include "sbz_physics.cuh"
+#include "sbz_table.cuh"
 #include "../../include/symboltz_gb300.h"
 
 namespace sbz {
 
 // Number of doubles per table node: (value, d/dτ) pairs of
 //   a, ℋ, κ̇, c_s² (chain rule through the background spline), e^{-κ}, κ̈, κ⃛ (Taylor mode).
-constexpr int kTabStride = 14;
-
-struct BgKnot { double t, y[5], s[5]; };  // time, unknowns, spline slopes
+constexpr int kTabStride = kTabValues;
 
 struct Background {
   Cosmo P;
@@ -22,7 +21,7 @@ struct Background {
   // coefficient table: ln τ uniform on [ln tau_start, ln tau0]
   int ntab = 0;
   double lnt0 = 0, dlnt = 0;
-  std::vector<double> tab;     // ntab * kTabStride
+  std::vector<double> tab;     // ntab * kTabStride; empty until background_table_values
   std::vector<double> tabtau;  // ntab node times
 };
 
@@ -30,7 +29,11 @@ int momentum_quadrature(int N, double* x, double* W);
 void cosmo_derive(Cosmo& P, const sbz_params& p, const sbz_model& m);
 // Solves one cosmology; returns 0 on success or an SBZ_* status code.
 int background_solve(Background& B, const sbz_params& p, const sbz_model& m, const sbz_opts& o);
-void background_table(Background& B, int ntab);
+// Node times of the coefficient table (cheap); the values are built by background_table_values on
+// the host or by the device kernel (sbz_table.cu) from the knots.
+void background_table_grid(Background& B, int ntab);
+void background_table_values(Background& B);
+inline void background_table(Background& B, int ntab) { background_table_grid(B, ntab); background_table_values(B); }
 // Spline of the unknowns at τ (value only)
 void background_spline(const Background& B, double tau, double* y);
 // Derived quantities at τ: a, ℋ, κ̇, κ, v, v̇, c_s², Xe, Tb (from the spline)

@@ -104,6 +104,13 @@ int los_weights(const double* taus, int ntau, std::vector<double>& chi, std::vec
 
 }  // namespace
 
+namespace sbz {
+// device build of the coefficient tables (sbz_table.cu)
+int table_build_launch(int ntab, int ncos, const Cosmo* d_cosmo, const BgKnot* d_knots, const int* d_koff, const int* d_nknot,
+                       const double* d_kappa0, const double* d_tabtau, const int* d_ok, double* d_tab, long long stride,
+                       cudaStream_t stream);
+}  // namespace sbz
+
 struct sbz_problem {
   sbz_model model{};
   sbz_opts opts{};
@@ -122,6 +129,7 @@ struct sbz_problem {
   DevBuf d_k, d_ti, d_cosmo, d_order, d_taus, d_out, d_status, d_steps;
   DevBuf c_y, c_yf, c_iv, c_cp, c_id, c_z, c_Sf, c_Sp, c_ks, c_ls, c_Th, c_Thp, c_P0, c_cz, c_cl, c_pa, c_pb, c_src, c_M,
       c_chi, c_w, c_taus, c_kf;
+  DevBuf t_cos, t_knots, t_koff, t_nknot, t_kap, t_tau, t_ok;  // inputs of the device table build
   int64_t table_stride = 0;
   bool own_stream = true;
   cudaEvent_t ev[12] = {};
@@ -228,7 +236,8 @@ void sbz_problem_destroy(sbz_problem* pb) {
     b->release();
   for (DevBuf* b : {&pb->c_y, &pb->c_yf, &pb->c_iv, &pb->c_cp, &pb->c_id, &pb->c_z, &pb->c_Sf, &pb->c_Sp, &pb->c_ks, &pb->c_ls,
                     &pb->c_Th, &pb->c_Thp, &pb->c_P0, &pb->c_cz, &pb->c_cl, &pb->c_pa, &pb->c_pb, &pb->c_src, &pb->c_M, &pb->c_chi,
-                    &pb->c_w, &pb->c_taus, &pb->c_kf})
+                    &pb->c_w, &pb->c_taus, &pb->c_kf, &pb->t_cos, &pb->t_knots, &pb->t_koff, &pb->t_nknot, &pb->t_kap, &pb->t_tau,
+                    &pb->t_ok})
     b->release();
   for (auto& e : pb->ev) if (e) cudaEventDestroy(e);
   if (pb->stream && pb->own_stream) cudaStreamDestroy(pb->stream);
@@ -252,7 +261,7 @@ int sbz_solve_bg(sbz_problem* pb, double* tau0, double* kappa0, double* taurec, 
     bo.maxiters = 100000;  // solvebg keeps its own iteration cap; opts.maxiters applies to the modes
     int st = sbz::background_solve(B, pb->params[c], pb->model, bo);
     if (st == SBZ_OK) {
-      sbz::background_table(B, ntab);
+      sbz::background_table_grid(B, ntab);  // node values: on the device at upload (or on demand on the host)
       st = sbz::build_cosmo(B, pb->M, pb->model, pb->cds[c]);
     }
     pb->bg_status[c] = st;
@@ -276,34 +285,53 @@ static int upload_tables(sbz_problem* pb) {
   if (r != SBZ_OK) return r;
   const int nc = pb->ncosmo;
   const int ntab = pb->opts.table_points;
-  // upload descriptors and tables (failed cosmologies get a flat dummy table)
+  // descriptors, then the tables built on the device from each cosmology's knots and node times
+  // (failed cosmologies get a flat dummy table)
   pb->table_stride = (int64_t)ntab * sbz::kNodeStride;
-  std::vector<double> tabs((size_t)nc * pb->table_stride, 0.0);
+  std::vector<sbz::Cosmo> cos(nc);
+  std::vector<int> koff(nc, 0), nknot(nc, 0), ok(nc, 0);
+  std::vector<double> kap(nc, 0.0), ttau((size_t)nc * ntab, 0.0);
+  std::vector<sbz::BgKnot> knots;
   for (int c = 0; c < nc; ++c) {
     const sbz::Background& B = pb->bgs[c];
-    double* T = &tabs[(size_t)c * pb->table_stride];
     if (pb->bg_status[c] != SBZ_OK) {
       sbz::CosmoDesc& D = pb->cds[c];
       std::memset(&D, 0, sizeof D);
       D.tau_start = D.tau0 = NAN; D.ntab = ntab; D.idlnt = 1;
       continue;
     }
-    for (int g = 0; g < ntab; ++g) {
-      double* nd = T + (size_t)g * sbz::kNodeStride;
-      nd[0] = B.tabtau[g];
-      nd[1] = (g + 1 < ntab) ? 1.0 / (B.tabtau[g + 1] - B.tabtau[g]) : 0.0;
-      std::memcpy(nd + 2, &B.tab[(size_t)g * sbz::kTabStride], sizeof(double) * sbz::kTabStride);
-    }
+    cos[c] = B.P; kap[c] = B.kappa0; ok[c] = 1;
+    koff[c] = (int)knots.size(); nknot[c] = (int)B.knots.size();
+    knots.insert(knots.end(), B.knots.begin(), B.knots.end());
+    std::memcpy(&ttau[(size_t)c * ntab], B.tabtau.data(), sizeof(double) * ntab);
   }
+  if (knots.empty()) knots.resize(1);
+  SBZ_CUDA(pb->t_cos.ensure(sizeof(sbz::Cosmo) * nc));
+  SBZ_CUDA(pb->t_knots.ensure(sizeof(sbz::BgKnot) * knots.size()));
+  SBZ_CUDA(pb->t_koff.ensure(sizeof(int) * nc));
+  SBZ_CUDA(pb->t_nknot.ensure(sizeof(int) * nc));
+  SBZ_CUDA(pb->t_ok.ensure(sizeof(int) * nc));
+  SBZ_CUDA(pb->t_kap.ensure(sizeof(double) * nc));
+  SBZ_CUDA(pb->t_tau.ensure(sizeof(double) * ttau.size()));
+  SBZ_CUDA(pb->d_tables.ensure(sizeof(double) * (size_t)nc * pb->table_stride));
+  SBZ_CUDA(cudaMemcpyAsync(pb->t_cos.p, cos.data(), sizeof(sbz::Cosmo) * nc, cudaMemcpyHostToDevice, pb->stream));
+  SBZ_CUDA(cudaMemcpyAsync(pb->t_knots.p, knots.data(), sizeof(sbz::BgKnot) * knots.size(), cudaMemcpyHostToDevice, pb->stream));
+  SBZ_CUDA(cudaMemcpyAsync(pb->t_koff.p, koff.data(), sizeof(int) * nc, cudaMemcpyHostToDevice, pb->stream));
+  SBZ_CUDA(cudaMemcpyAsync(pb->t_nknot.p, nknot.data(), sizeof(int) * nc, cudaMemcpyHostToDevice, pb->stream));
+  SBZ_CUDA(cudaMemcpyAsync(pb->t_ok.p, ok.data(), sizeof(int) * nc, cudaMemcpyHostToDevice, pb->stream));
+  SBZ_CUDA(cudaMemcpyAsync(pb->t_kap.p, kap.data(), sizeof(double) * nc, cudaMemcpyHostToDevice, pb->stream));
+  SBZ_CUDA(cudaMemcpyAsync(pb->t_tau.p, ttau.data(), sizeof(double) * ttau.size(), cudaMemcpyHostToDevice, pb->stream));
+  if (sbz::table_build_launch(ntab, nc, pb->t_cos.as<sbz::Cosmo>(), pb->t_knots.as<sbz::BgKnot>(), pb->t_koff.as<int>(),
+                              pb->t_nknot.as<int>(), pb->t_kap.as<double>(), pb->t_tau.as<double>(), pb->t_ok.as<int>(),
+                              pb->d_tables.as<double>(), pb->table_stride, pb->stream) != SBZ_OK)
+    return fail(SBZ_ERR_CUDA, "coefficient table build");
   SBZ_CUDA(pb->d_model.ensure(sizeof(sbz::ModelDesc)));
   SBZ_CUDA(pb->d_comps.ensure(sizeof(sbz::CompDesc) * pb->comps.size()));
   SBZ_CUDA(pb->d_cosmos.ensure(sizeof(sbz::CosmoDesc) * nc));
-  SBZ_CUDA(pb->d_tables.ensure(sizeof(double) * tabs.size()));
   SBZ_CUDA(pb->d_counter.ensure(sizeof(unsigned)));
   SBZ_CUDA(cudaMemcpyAsync(pb->d_model.p, &pb->M, sizeof(sbz::ModelDesc), cudaMemcpyHostToDevice, pb->stream));
   SBZ_CUDA(cudaMemcpyAsync(pb->d_comps.p, pb->comps.data(), sizeof(sbz::CompDesc) * pb->comps.size(), cudaMemcpyHostToDevice, pb->stream));
   SBZ_CUDA(cudaMemcpyAsync(pb->d_cosmos.p, pb->cds.data(), sizeof(sbz::CosmoDesc) * nc, cudaMemcpyHostToDevice, pb->stream));
-  SBZ_CUDA(cudaMemcpyAsync(pb->d_tables.p, tabs.data(), sizeof(double) * tabs.size(), cudaMemcpyHostToDevice, pb->stream));
   SBZ_CUDA(cudaStreamSynchronize(pb->stream));
   pb->tables_uploaded = true;
   return SBZ_OK;
@@ -328,7 +356,9 @@ int sbz_bg_eval(const sbz_problem* pb, int cosmo, int n, const double* tau, doub
 
 int sbz_bg_coefficients(const sbz_problem* pb, int cosmo, int n, const double* tau, double* out7) {
   if (!pb || !pb->bg_done || cosmo < 0 || cosmo >= pb->ncosmo || pb->bg_status[cosmo] != SBZ_OK) return fail(SBZ_ERR_STATE, "background not solved");
-  const sbz::Background& B = pb->bgs[cosmo];
+  // the kernels' table is built on the device; the host copy of its values is built on first use
+  sbz::Background& B = const_cast<sbz::Background&>(pb->bgs[cosmo]);
+  if (B.tab.empty()) sbz::background_table_values(B);
   for (int i = 0; i < n; ++i) sbz::table_eval(B, tau[i], out7 + 7 * i);
   return SBZ_OK;
 }
