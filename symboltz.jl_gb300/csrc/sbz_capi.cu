@@ -356,9 +356,27 @@ int sbz_bg_eval(const sbz_problem* pb, int cosmo, int n, const double* tau, doub
 
 int sbz_bg_coefficients(const sbz_problem* pb, int cosmo, int n, const double* tau, double* out7) {
   if (!pb || !pb->bg_done || cosmo < 0 || cosmo >= pb->ncosmo || pb->bg_status[cosmo] != SBZ_OK) return fail(SBZ_ERR_STATE, "background not solved");
-  // the kernels' table is built on the device; the host copy of its values is built on first use
-  sbz::Background& B = const_cast<sbz::Background&>(pb->bgs[cosmo]);
-  if (B.tab.empty()) sbz::background_table_values(B);
+  // The kernels' table is built on the device.  The host copy of its values is made on first use:
+  // downloaded from the device when there is one (bit-identical to what the kernels read),
+  // otherwise built on the host from the same table_node code.
+  sbz_problem* pm = const_cast<sbz_problem*>(pb);
+  sbz::Background& B = pm->bgs[cosmo];
+  if (B.tab.empty()) {
+    int dev = 0;
+    bool got = false;
+    if (cudaGetDevice(&dev) == cudaSuccess && upload_tables(pm) == SBZ_OK) {
+      std::vector<double> nodes((size_t)pm->table_stride);
+      if (cudaMemcpyAsync(nodes.data(), pm->d_tables.as<double>() + (size_t)cosmo * pm->table_stride, sizeof(double) * nodes.size(),
+                          cudaMemcpyDeviceToHost, pm->stream) == cudaSuccess &&
+          cudaStreamSynchronize(pm->stream) == cudaSuccess) {
+        B.tab.resize((size_t)B.ntab * sbz::kTabStride);
+        for (int g = 0; g < B.ntab; ++g)
+          std::memcpy(&B.tab[(size_t)g * sbz::kTabStride], &nodes[(size_t)g * sbz::kNodeStride + 2], sizeof(double) * sbz::kTabStride);
+        got = true;
+      }
+    }
+    if (!got) { cudaGetLastError(); sbz::background_table_values(B); }
+  }
   for (int i = 0; i < n; ++i) sbz::table_eval(B, tau[i], out7 + 7 * i);
   return SBZ_OK;
 }
