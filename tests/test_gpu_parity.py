@@ -328,3 +328,19 @@ def test_plain_lcdm_fp64_rtol1e6(S):
     for s in range(3):
         scale = np.max(np.abs(ref[:, :, s]), axis=1, keepdims=True) + 1e-300
         assert np.max(np.abs(out[:, :, s] - ref[:, :, s]) / scale) < 1e-3, s
+
+
+def test_device_table_matches_oracle(S, bg5):
+    """The coefficient table built on the device (what the kernels read; bg.coefficients serves it)
+    against the oracle's background, at the tolerances the host build is held to on CPU."""
+    M = S.ΛCDM(lmax=5)
+    p = S.CosmologyProblem(M, S.parameters_Planck18(M))
+    bg = p.solvebg()
+    ts = np.geomspace(1e-6 * 1.01, bg5.tau0 * (1 - 1e-9), 400)
+    c, b = bg.coefficients(ts), bg5.eval(ts)
+    for q, j, tol in ((0, 0, 1e-7), (1, 1, 1e-7), (2, 2, 2e-6)):  # a, ℋ, κ̇
+        np.testing.assert_allclose(c[:, q], b[:, j], rtol=tol)
+    np.testing.assert_allclose(c[:, 3], b[:, 6], rtol=1e-5)  # c_s²
+    ek = np.exp(-b[:, 3])  # e^{-κ} from the oracle's κ, where the sources see it (early on κ is huge)
+    seen = ek > 1e-3
+    np.testing.assert_allclose(c[seen, 4], ek[seen], rtol=1e-5)
