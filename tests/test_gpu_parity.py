@@ -340,7 +340,9 @@ def test_device_table_matches_oracle(S, bg5):
     c, b = bg.coefficients(ts), bg5.eval(ts)
     for q, j, tol in ((0, 0, 1e-7), (1, 1, 1e-7), (2, 2, 2e-6)):  # a, ℋ, κ̇
         np.testing.assert_allclose(c[:, q], b[:, j], rtol=tol)
-    np.testing.assert_allclose(c[:, 3], b[:, 6], rtol=1e-5)  # c_s²
+    # c_s² follows the slopes of the stiff ΔT spline: where it is ~4e-9 the background solved on an
+    # aarch64 host differs from the x86 oracle fixture's by ~1.5e-5 (4.5e-6 on x86)
+    np.testing.assert_allclose(c[:, 3], b[:, 6], rtol=5e-5)
     ek = np.exp(-b[:, 3])  # e^{-κ} from the oracle's κ, where the sources see it (early on κ is huge)
     seen = ek > 1e-3
     np.testing.assert_allclose(c[seen, 4], ek[seen], rtol=1e-5)
