@@ -208,7 +208,7 @@ int sbz_autotune_pt(sbz_problem* pb, int nk, const int* cosmo, const double* ks,
 int sbz_mlp_gemm(int M, int N, int K, const void* A, const void* B, int epi, int act, const float* bias, void* out, int ldo,
                  int n_valid, int accumulate, void* z_out, const void* z_in, void* stream);
 
-/* Source surrogate (sbz_surrogate_*; SURVEY-specified learned part, no counterpart in the reference):
+/* Source surrogate (sbz_surrogate_*; a learned part with no counterpart in the reference):
  * an MLP nin → nhidden × width (SiLU) → nout trained and evaluated with the BF16 tensor-core GEMM
  * above (FP32 accumulation, FP32 master weights, Adam, MSE loss on the caller's normalised targets).
  * nin, nout ≤ 64, width % 128 == 0, batch % 128 == 0.  Inputs/targets are host float arrays
