@@ -95,6 +95,9 @@ def test_parameter_updates_equal_fresh_problems():
     assert p.ncosmo == 3 and len(bg.tau0) == 3
     for i, (h, oc) in enumerate(rows):
         assert bg.tau0[i] == S.CosmologyProblem(M, dict(base, h=h, Omega_c=oc)).solvebg().tau0[0]
+    with pytest.raises(S.SbzError):  # the C-ABI refuses an empty parameter set
+        S._lib.check(S._lib.lib().sbz_problem_set_params(p._h, None, 0), "set_params")
+    assert p.solvebg().tau0.shape == (3,)  # and leaves the problem as it was
     with pytest.raises(KeyError):
         S.parameter_updater(p, ["H0"])
     with pytest.raises(ValueError):
