@@ -1,8 +1,8 @@
 /* symboltz_gb300: C-ABI of the GB300 perturbation + line-of-sight engine.
  *
  * Drop-in for the hot path of hersle/SymBoltz.jl.  Each entry point names the reference
- * function (file:line inside the SymBoltz.jl repository) whose behaviour it replaces; the
- * Julia/Python bindings that call these are shown in INTEGRATION.md.
+ * function (file:line inside the SymBoltz.jl repository) whose behaviour it replaces; a Julia
+ * module binds them with ccall, the Python package symboltz with ctypes.
  *
  * Conventions: plain pointers and sizes; host pointers unless the name ends in _device;
  * integer status returns (0 = ok, < 0 = argument/CUDA errors, see SBZ_ERR_*); per-mode solver
@@ -244,8 +244,9 @@ int sbz_cl_integrate(int nk, const double* ks, const double* P0, int nl, const d
  * are device pointers; the work is queued on `stream` (NULL: the default stream) and the call
  * returns without waiting.  Scratch is a fixed SBZ_NOALLOC_SCRATCH_DOUBLES-double device array:
  * sizes with 2*ceil32(nk+1) + (nk+1)*nl above it return SBZ_ERR_ARG.  All calls share that array
- * (it keeps the last call's contents), so calls that overlap on the GPU race.  The first call on
- * each device looks up the array's address; make it before any stream capture.  Knots that are not
+ * (it keeps the last call's contents), so calls that overlap on the GPU race.  Every call looks up
+ * the array's address in the current context; the first call on a device also loads the module
+ * there, so make it before any stream capture.  Knots that are not
  * positive and increasing give NaN C_l (the host does not read device inputs). */
 #define SBZ_NOALLOC_SCRATCH_DOUBLES 2097152
 int sbz_cl_integrate_noalloc(int nk, const double* d_ks, const double* d_P0, int nl, const double* d_ThA,

@@ -32,7 +32,12 @@ typedef struct orc_opts {
   double tau_ini, tau_max;      /* background integration span (src/solve.jl:131 ivspan) */
   long maxiters;
   int nthreads;
+  int alg_bg, alg_pt;           /* ORC_RODAS4 or ORC_RODAS5P for the background / perturbations */
+  int pt_linsolve;              /* ORC_LINSOLVE_DENSE (the checker) or ORC_LINSOLVE_SPARSE (CPU baseline) */
 } orc_opts;
+
+enum { ORC_RODAS4 = 0, ORC_RODAS5P = 1 };
+enum { ORC_LINSOLVE_DENSE = 0, ORC_LINSOLVE_SPARSE = 1 };
 
 /* Background solution handle. */
 typedef struct orc_bg orc_bg;

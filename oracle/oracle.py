@@ -39,7 +39,12 @@ class Model(C.Structure):
 class Opts(C.Structure):
     _fields_ = [("bg_rtol", C.c_double), ("bg_atol", C.c_double), ("pt_rtol", C.c_double),
                 ("pt_atol", C.c_double), ("tau_ini", C.c_double), ("tau_max", C.c_double),
-                ("maxiters", C.c_long), ("nthreads", C.c_int)]
+                ("maxiters", C.c_long), ("nthreads", C.c_int), ("alg_bg", C.c_int), ("alg_pt", C.c_int),
+                ("pt_linsolve", C.c_int)]
+
+
+RODAS4, RODAS5P = 0, 1
+_ALGS = {"rodas4": RODAS4, "rodas5p": RODAS5P}
 
 
 _lib = None
@@ -165,11 +170,15 @@ class Background:
     """Background + thermodynamics solution of one cosmology (src/solve.jl:427-435)."""
 
     def __init__(self, params: dict, model: dict, *, bg_rtol=1e-7, bg_atol=1e-7, pt_rtol=1e-5,
-                 pt_atol=1e-5, tau_ini=1e-6, tau_max=100.0, maxiters=100000):
+                 pt_atol=1e-5, tau_ini=1e-6, tau_max=100.0, maxiters=100000, alg="rodas5p", bg_alg="rodas4",
+                 linsolve="dense"):
+        """linsolve: "dense" (LU with partial pivoting, the checker) or "sparse" (the reference's
+        sparse-LU path restated, used as the timed CPU baseline)."""
         self.params, self.model = dict(params), dict(model)
         self.p = Params(**params)
         self.m = Model(**model)
-        self.o = Opts(bg_rtol, bg_atol, pt_rtol, pt_atol, tau_ini, tau_max, maxiters, 0)
+        self.o = Opts(bg_rtol, bg_atol, pt_rtol, pt_atol, tau_ini, tau_max, maxiters, 0, _ALGS[bg_alg], _ALGS[alg],
+                      {"dense": 0, "sparse": 1}[linsolve])
         st = C.c_int(0)
         self.h = lib().orc_bg_solve(C.byref(self.p), C.byref(self.m), C.byref(self.o), C.byref(st))
         self.status = st.value

@@ -13,9 +13,10 @@
 //   background solve     src/solve.jl:158-203 (a=1 callback), 427-435
 //   background spline    src/utils.jl:118-127 (cubic Hermite spline of the bg unknowns)
 //   perturbation solve   src/solve.jl:496-569
-// The integrator is the Hairer-Wanner RODAS (order 4(3), stiffly accurate, L-stable)
-// Rosenbrock method.  The reference uses Rodas5P from OrdinaryDiffEqRosenbrock (not vendored);
-// parity with it is at the level of outputs, not steps.  Linear systems are solved with dense
+// The integrator is a Rosenbrock method in transformed form: Rodas5P (Steinebach 2023, order
+// 5(4)), the reference's default (src/solve.jl:320,339; OrdinaryDiffEqRosenbrock, not vendored,
+// restated from the published tableau), or the Hairer-Wanner RODAS (order 4(3)).  Parity with
+// the reference is at the level of outputs, not steps.  Linear systems are solved with dense
 // LU and partial pivoting (the reference uses KLU on the same matrix).
 #include "oracle.h"
 #include "jet.hpp"
@@ -145,6 +146,7 @@ struct Cosmo {
   double xq[16], Wq[16], dlnf[16];
   double rtol_bg, atol_bg, rtol_pt, atol_pt, tau_ini, tau_max;
   long maxiters;
+  int alg_bg, alg_pt, pt_linsolve;
 };
 
 static void cosmo_init(Cosmo& P, const orc_params* p, const orc_model* m, const orc_opts* o) {
@@ -158,7 +160,7 @@ static void cosmo_init(Cosmo& P, const orc_params* p, const orc_model* m, const 
   P.Og0 = PI * PI / 15 * std::pow(kB * P.T0, 4) / (std::pow(hbar, 3) * std::pow(c, 5)) * 8 * PI * GN / (3 * P.H0si * P.H0si);
   // massless nu: src/models/cosmologies.jl:78-81
   P.On0 = P.Neff * 7.0 / 8.0 * std::pow(4.0 / 11.0, 4.0 / 3.0) * P.Og0;
-  // massive nu: src/models/neutrinos.jl:262-281
+  // massive nu: src/models/neutrinos.jl:78-86
   P.Oh0 = 0; P.Th0 = std::pow(4.0 / 11.0, 1.0 / 3.0) * P.T0; P.y0 = 0; P.Irho0 = 0;
   if (P.nx > 0) {
     momentum_quadrature(P.nx, P.xq, P.Wq);
@@ -172,11 +174,12 @@ static void cosmo_init(Cosmo& P, const orc_params* p, const orc_model* m, const 
   }
   // closure on the last species (Lambda): src/models/cosmologies.jl:221-227
   P.OL0 = 1 - (P.Og0 + P.On0 + P.Oc0 + P.Ob0 + P.Oh0);
-  // src/models/baryons.jl:151, src/models/inflation.jl:218
+  // src/models/baryons.jl:151, src/models/inflation.jl:6
   P.fHe = P.YHe / (mHe / mH * (1 - P.YHe));
   P.kpivot = 0.05 / Mpc / (H100 / c) / P.h;
   P.rtol_bg = o->bg_rtol; P.atol_bg = o->bg_atol; P.rtol_pt = o->pt_rtol; P.atol_pt = o->pt_atol;
   P.tau_ini = o->tau_ini; P.tau_max = o->tau_max; P.maxiters = o->maxiters;
+  P.alg_bg = o->alg_bg; P.alg_pt = o->alg_pt; P.pt_linsolve = o->pt_linsolve;
 }
 
 template <class S> inline S smoothifelse(const S& x, const S& v1, const S& v2, double k) {
@@ -296,32 +299,126 @@ static void bg_rhs(const Cosmo& P, const S* y, S* dy, BgOut<S>* out) {
 }
 
 // ------------------------------------------------------------------------------------------
-// Rosenbrock integrator: Hairer-Wanner RODAS (order 4, embedded 3), transformed form
-//   (1/(h g) I - J) U_i = f(t + c_i h, y + sum_j A_ij U_j) + sum_j (C_ij/h) U_j + h d_i f_t
-//   y1 = y + sum_j A_5j U_j + U_5 + U_6,  error estimate U_6.
-namespace RW {
-const double gam = 0.25;
-const double c2 = 0.386, c3 = 0.21, c4 = 0.63;
-const double d1 = 0.25, d2 = -0.1043, d3 = 0.1035, d4 = -0.0362;
-const double a21 = 1.544;
-const double a31 = 0.9466785280815826, a32 = 0.2557011698983284;
-const double a41 = 3.314825187068521, a42 = 2.896124015972201, a43 = 0.9986419139977817;
-const double a51 = 1.221224509226641, a52 = 6.019134481288629, a53 = 12.53708332932087, a54 = -0.6878860361058950;
-const double c21 = -5.6688;
-const double c31 = -2.430093356833875, c32 = -0.2063599157091915;
-const double c41 = -0.1073529058151375, c42 = -9.594562251023355, c43 = -20.47028614809616;
-const double c51 = 7.496443313967647, c52 = -10.24680431464352, c53 = -33.99990352819905, c54 = 11.70890893206160;
-const double c61 = 8.083246795921522, c62 = -7.981132988064893, c63 = -31.52159432874371, c64 = 16.31930543123136, c65 = -6.058818238834054;
-}  // namespace RW
+// Rosenbrock tableaus in the transformed (W = 1/(h gamma) I - J) form of Hairer & Wanner,
+// Solving ODEs II, IV.7 (eq. 7.25):
+//   W U_i = f(t + c_i h, y + sum_j A_ij U_j) + sum_j (C_ij / h) U_j + h d_i f_t,
+//   y1 = y + sum_j m_j U_j,  error estimate = U_s (the last stage; the embedded solution omits it).
+// Step-size control is the PI controller fac = 0.9 err^-beta1 errold^beta2 (clamped to [0.2, 10]),
+// with rejections scaled by max(0.2, 0.9 err^-rej).
+// Dense output (ndense = 3): y(t + θh) = (1-θ) y + θ (y1 + (1-θ)(K0 + θ K1 + θ² K2)) with
+// K_r = sum_j H_rj U_j; ndense = 0: cubic Hermite through (y, f) at both ends.
+struct Tableau {
+  int s;
+  double c[8], d[8], A[8][8], C[8][8], m[8];
+  double beta1, beta2, rej;
+  int ndense;
+  double H[3][8];
+};
 
+// RODAS (Hairer & Wanner, order 4(3), stiffly accurate): 6 stages.
+static Tableau make_rodas4() {
+  Tableau T{};
+  T.s = 6;
+  const double c2 = 0.386, c3 = 0.21, c4 = 0.63;
+  const double a21 = 1.544;
+  const double a31 = 0.9466785280815826, a32 = 0.2557011698983284;
+  const double a41 = 3.314825187068521, a42 = 2.896124015972201, a43 = 0.9986419139977817;
+  const double a51 = 1.221224509226641, a52 = 6.019134481288629, a53 = 12.53708332932087, a54 = -0.6878860361058950;
+  const double Cs[6][6] = {{0}, {-5.6688}, {-2.430093356833875, -0.2063599157091915},
+                           {-0.1073529058151375, -9.594562251023355, -20.47028614809616},
+                           {7.496443313967647, -10.24680431464352, -33.99990352819905, 11.70890893206160},
+                           {8.083246795921522, -7.981132988064893, -31.52159432874371, 16.31930543123136, -6.058818238834054}};
+  const double cs[6] = {0, c2, c3, c4, 1, 1}, ds[6] = {0.25, -0.1043, 0.1035, -0.0362, 0, 0};
+  for (int i = 0; i < 6; ++i) { T.c[i] = cs[i]; T.d[i] = ds[i]; for (int j = 0; j < i; ++j) T.C[i][j] = Cs[i][j]; }
+  T.A[1][0] = a21; T.A[2][0] = a31; T.A[2][1] = a32; T.A[3][0] = a41; T.A[3][1] = a42; T.A[3][2] = a43;
+  const double a5[4] = {a51, a52, a53, a54};
+  for (int j = 0; j < 4; ++j) { T.A[4][j] = a5[j]; T.A[5][j] = a5[j]; T.m[j] = a5[j]; }
+  T.A[5][4] = 1; T.m[4] = 1; T.m[5] = 1;
+  T.beta1 = 0.175; T.beta2 = 0.1; T.rej = 0.25;
+  return T;
+}
+
+// Rodas5P (Steinebach 2023, order 5(4), stiffly accurate; the reference's default integrator,
+// src/solve.jl:320,339): 8 stages; stages 6-8 at t + h, each adding one correction.  The PI
+// exponents are OrdinaryDiffEq's defaults for an order-5 method (7/50, 2/25), rejections by
+// 0.9 err^-7/50.
+static Tableau make_rodas5p() {
+  Tableau T{};
+  T.s = 8;
+  const double gam = 0.21193756319429014;
+  const double cs[8] = {0, 0.6358126895828704, 0.4095798393397535, 0.9769306725060716, 0.4288403609558664, 1, 1, 1};
+  const double ds[8] = {gam, -0.42387512638858027, -0.3384627126235924, 1.8046452872882734, 2.325825639765069, 0, 0, 0};
+  const double As[6][5] = {{0},
+                           {3.0},
+                           {2.849394379747939, 0.45842242204463923},
+                           {-6.954028509809101, 2.489845061869568, -10.358996098473584},
+                           {2.8029986275628964, 0.5072464736228206, -0.3988312541770524, -0.04721187230404641},
+                           {-7.502846399306121, 2.561846144803919, -11.627539656261098, -0.18268767659942256, 0.030198172008377946}};
+  const double Cs[8][7] = {{0},
+                           {-14.155112264123755},
+                           {-17.97296035885952, -2.859693295451294},
+                           {147.12150275711716, -1.41221402718213, 71.68940251302358},
+                           {165.43517024871676, -0.4592823456491126, 42.90938336958603, -5.961986721573306},
+                           {24.854864614690072, -3.0009227002832186, 47.4931110020768, 5.5814197821558125, -0.6610691825249471},
+                           {30.91273214028599, -3.1208243349937974, 77.79954646070892, 34.28646028294783, -19.097331116725623,
+                            -28.087943162872662},
+                           {37.80277123390563, -3.2571969029072276, 112.26918849496327, 66.9347231244047, -40.06618937091002,
+                            -54.66780262877968, -9.48861652309627}};
+  for (int i = 0; i < 8; ++i) { T.c[i] = cs[i]; T.d[i] = ds[i]; for (int j = 0; j < i; ++j) T.C[i][j] = Cs[i][j]; }
+  for (int i = 1; i < 6; ++i) for (int j = 0; j < i; ++j) T.A[i][j] = As[i][j];
+  for (int j = 0; j < 5; ++j) { T.A[6][j] = As[5][j]; T.A[7][j] = As[5][j]; T.m[j] = As[5][j]; }
+  T.A[6][5] = 1; T.A[7][5] = 1; T.A[7][6] = 1; T.m[5] = 1; T.m[6] = 1; T.m[7] = 1;
+  T.beta1 = 0.14; T.beta2 = 0.08; T.rej = 0.14;
+  // Continuous extension of order 4, derived for this tableau: the eight tree conditions of order
+  // <= 4 of a Rosenbrock method with θ-dependent weights, sum_j b_j(θ) Φ_j(t) = P_t(θ) (P_t(1) =
+  // the usual right-hand sides, e.g. θ²/2 - γθ for the second-order tree), are linear in H for the
+  // form above and have rank 6 in the 7 non-error stages; one more condition, H u∞ = 0 with u∞
+  // the stages of y' = λy as hλ → -∞, makes stiff components interpolate linearly between the
+  // step ends instead of being amplified (tight coupling).  Those 7 conditions fix H.
+  // (The reference's own Rodas5P interpolant is a different continuous extension.)
+  T.ndense = 3;
+  const double Hs[3][7] = {
+      {16.487964434865184, -2.370717139483559, -36.89699909384169, -47.19777482102162, 29.31762179544809, 37.62133721923128, 6.977388062974808},
+      {21.885022549967175, -1.5984168138259751, 162.13711388885017, 126.19157982265247, -76.60482233539331, -106.69765784722038, -28.805926606943324},
+      {-15.646484681406143, 3.423681775524067, -62.48695397162234, -48.12822622663184, 30.299848310633063, 44.62468119063477, 18.5833010918263}};
+  for (int r = 0; r < 3; ++r) for (int j = 0; j < 7; ++j) T.H[r][j] = Hs[r][j];
+  return T;
+}
+
+static const Tableau& tableau(int alg) {
+  static const Tableau r4 = make_rodas4(), r5 = make_rodas5p();
+  return alg == ORC_RODAS5P ? r5 : r4;
+}
+// gamma of the tableaus (the diagonal of W)
+static double tableau_gamma(int alg) { return alg == ORC_RODAS5P ? 0.21193756319429014 : 0.25; }
+
+static bool lu_factor(int n, double* A, int* piv);
+static void lu_solve(int n, const double* A, const int* piv, double* b);
+
+// An ODE system with its Rosenbrock linear algebra: w_factor forms and factors W = ihg I - J(t, y)
+// and returns ∂f/∂t; w_solve applies W⁻¹ in place.  The defaults use the dense J of jac() and
+// dense LU with partial pivoting.
 struct OdeSys {
   int n;
   virtual void rhs(double t, const double* y, double* f) = 0;
   virtual void jac(double t, const double* y, double* J, double* ft) = 0;  // J row-major n x n
+  virtual bool w_factor(double t, const double* y, double ihg, double* ft) {
+    Jd_.resize((size_t)n * n); W_.resize((size_t)n * n); piv_.resize(n);
+    jac(t, y, Jd_.data(), ft);
+    for (size_t i = 0; i < W_.size(); ++i) W_[i] = -Jd_[i];
+    for (int i = 0; i < n; ++i) W_[(size_t)i * n + i] += ihg;
+    return lu_factor(n, W_.data(), piv_.data());
+  }
+  virtual void w_solve(double* b) { lu_solve(n, W_.data(), piv_.data(), b); }
   virtual ~OdeSys() {}
+ private:
+  std::vector<double> Jd_, W_;
+  std::vector<int> piv_;
 };
 struct StepSink {
-  virtual bool on_step(double t0, const double* y0, const double* f0, double t1, const double* y1, const double* f1) = 0;
+  // K: the tableau's dense-output vectors (3 x n) or nullptr (cubic Hermite)
+  virtual bool on_step(double t0, const double* y0, const double* f0, double t1, const double* y1, const double* f1,
+                       const double* K) = 0;
   virtual ~StepSink() {}
 };
 
@@ -348,12 +445,13 @@ static void lu_solve(int n, const double* A, const int* piv, double* b) {
 
 enum { ST_OK = 0, ST_MAXITERS = 1, ST_DTMIN = 2, ST_NONFINITE = 3 };
 
-static int rodas4(OdeSys& sys, double t, double tf, double* y, double rtol, double atol, long maxiters,
-                  StepSink* sink, long* nacc, long* nrej) {
-  using namespace RW;
-  const int n = sys.n;
-  std::vector<double> f0(n), ft(n), J(n * n), W(n * n), U1(n), U2(n), U3(n), U4(n), U5(n), U6(n), Y(n), F(n), y1(n), f1(n);
-  std::vector<int> piv(n);
+static int rosenbrock(int alg, OdeSys& sys, double t, double tf, double* y, double rtol, double atol, long maxiters,
+                      StepSink* sink, long* nacc, long* nrej) {
+  const Tableau& T = tableau(alg);
+  const double gam = tableau_gamma(alg);
+  const int n = sys.n, S = T.s;
+  std::vector<double> f0(n), ft(n), Y(n), F(n), y1(n), f1(n), K(3 * n);
+  std::vector<std::vector<double>> U(S, std::vector<double>(n));
   *nacc = 0; *nrej = 0;
   if (!(tf > t)) return ST_OK;
   sys.rhs(t, y, f0.data());
@@ -376,70 +474,65 @@ static int rodas4(OdeSys& sys, double t, double tf, double* y, double rtol, doub
     h = std::min(100 * h0, h1);
     if (!std::isfinite(h) || h <= 0) h = 1e-6 * std::max(1.0, std::fabs(t));
   }
-  double errold = 1e-4; bool last_rejected = false; bool last_nonfinite = false;
+  const double kLogErrFloor = std::log(1e-4);  // the controller's floor on errold
+  double lerrold = kLogErrFloor; bool last_rejected = false; bool last_nonfinite = false;
   long iters = 0;
   while (t < tf) {
     if (++iters > maxiters) return ST_MAXITERS;
     if (t + h >= tf || t + 1.01 * h >= tf) h = tf - t;
     if (h < 1e-14 * std::max(std::fabs(t), 1e-300) || h <= 0) return last_nonfinite ? ST_NONFINITE : ST_DTMIN;
-    sys.jac(t, y, J.data(), ft.data());
     const double ihg = 1.0 / (h * gam), ih = 1.0 / h;
-    for (int i = 0; i < n * n; ++i) W[i] = -J[i];
-    for (int i = 0; i < n; ++i) W[i * n + i] += ihg;
-    bool ok = lu_factor(n, W.data(), piv.data());
-    double err = NAN;
+    bool ok = sys.w_factor(t, y, ihg, ft.data());
+    double err2 = NAN;
     if (ok) {
-      for (int i = 0; i < n; ++i) U1[i] = f0[i] + h * d1 * ft[i];
-      lu_solve(n, W.data(), piv.data(), U1.data());
-      for (int i = 0; i < n; ++i) Y[i] = y[i] + a21 * U1[i];
-      sys.rhs(t + c2 * h, Y.data(), F.data());
-      for (int i = 0; i < n; ++i) U2[i] = F[i] + ih * (c21 * U1[i]) + h * d2 * ft[i];
-      lu_solve(n, W.data(), piv.data(), U2.data());
-      for (int i = 0; i < n; ++i) Y[i] = y[i] + a31 * U1[i] + a32 * U2[i];
-      sys.rhs(t + c3 * h, Y.data(), F.data());
-      for (int i = 0; i < n; ++i) U3[i] = F[i] + ih * (c31 * U1[i] + c32 * U2[i]) + h * d3 * ft[i];
-      lu_solve(n, W.data(), piv.data(), U3.data());
-      for (int i = 0; i < n; ++i) Y[i] = y[i] + a41 * U1[i] + a42 * U2[i] + a43 * U3[i];
-      sys.rhs(t + c4 * h, Y.data(), F.data());
-      for (int i = 0; i < n; ++i) U4[i] = F[i] + ih * (c41 * U1[i] + c42 * U2[i] + c43 * U3[i]) + h * d4 * ft[i];
-      lu_solve(n, W.data(), piv.data(), U4.data());
-      for (int i = 0; i < n; ++i) Y[i] = y[i] + a51 * U1[i] + a52 * U2[i] + a53 * U3[i] + a54 * U4[i];
-      sys.rhs(t + h, Y.data(), F.data());
-      for (int i = 0; i < n; ++i) U5[i] = F[i] + ih * (c51 * U1[i] + c52 * U2[i] + c53 * U3[i] + c54 * U4[i]);
-      lu_solve(n, W.data(), piv.data(), U5.data());
-      for (int i = 0; i < n; ++i) Y[i] += U5[i];
-      sys.rhs(t + h, Y.data(), F.data());
-      for (int i = 0; i < n; ++i) U6[i] = F[i] + ih * (c61 * U1[i] + c62 * U2[i] + c63 * U3[i] + c64 * U4[i] + c65 * U5[i]);
-      lu_solve(n, W.data(), piv.data(), U6.data());
-      for (int i = 0; i < n; ++i) y1[i] = Y[i] + U6[i];
+      for (int st = 0; st < S; ++st) {
+        if (st == 0) {
+          for (int i = 0; i < n; ++i) U[0][i] = f0[i] + h * T.d[0] * ft[i];
+        } else {
+          for (int i = 0; i < n; ++i) { double v = y[i]; for (int j = 0; j < st; ++j) v += T.A[st][j] * U[j][i]; Y[i] = v; }
+          sys.rhs(t + T.c[st] * h, Y.data(), F.data());
+          for (int i = 0; i < n; ++i) {
+            double v = 0; for (int j = 0; j < st; ++j) v += T.C[st][j] * U[j][i];
+            U[st][i] = F[i] + ih * v + (T.d[st] != 0 ? h * T.d[st] * ft[i] : 0.0);
+          }
+        }
+        sys.w_solve(U[st].data());
+      }
+      for (int i = 0; i < n; ++i) { double v = y[i]; for (int j = 0; j < S; ++j) v += T.m[j] * U[j][i]; y1[i] = v; }
       double s = 0;
       for (int i = 0; i < n; ++i) {
         double sk = atol + rtol * std::max(std::fabs(y[i]), std::fabs(y1[i]));
-        s += (U6[i] / sk) * (U6[i] / sk);
+        s += (U[S - 1][i] / sk) * (U[S - 1][i] / sk);
       }
-      err = std::sqrt(s / n);
+      err2 = s / n;  // squared RMS error norm
     }
-    const double expo = 0.25, safety = 0.9, qmin = 0.2, qmax = 10.0;
-    if (std::isfinite(err) && err <= 1.0) {
+    const double qmin = 0.2, qmax = 10.0;
+    if (std::isfinite(err2) && err2 <= 1.0) {
       const double tnew = (h == tf - t) ? tf : t + h;
       sys.rhs(tnew, y1.data(), f1.data());
-      if (sink && !sink->on_step(t, y, f0.data(), tnew, y1.data(), f1.data())) return ST_OK;
+      const double* Kp = nullptr;
+      if (sink && T.ndense) {
+        for (int r = 0; r < T.ndense; ++r)
+          for (int i = 0; i < n; ++i) { double v = 0; for (int j = 0; j < S; ++j) v += T.H[r][j] * U[j][i]; K[r * n + i] = v; }
+        Kp = K.data();
+      }
+      if (sink && !sink->on_step(t, y, f0.data(), tnew, y1.data(), f1.data(), Kp)) return ST_OK;
       t = tnew;
       std::memcpy(y, y1.data(), n * sizeof(double));
       f0.swap(f1);
       ++*nacc;
-      double e = std::max(err, 1e-10);
-      double fac = safety * std::pow(e, -0.7 * expo) * std::pow(errold, 0.4 * expo);
+      const double lerr = 0.5 * std::log(std::max(err2, 1e-20));
+      double fac = 0.9 * std::exp(-T.beta1 * lerr + T.beta2 * lerrold);
       fac = std::min(qmax, std::max(qmin, fac));
       if (last_rejected) fac = std::min(fac, 1.0);
-      errold = std::max(err, 1e-4);
+      lerrold = std::max(lerr, kLogErrFloor);
       h *= fac;
       last_rejected = false; last_nonfinite = false;
     } else {
       ++*nrej;
       last_rejected = true;
-      if (!std::isfinite(err)) { last_nonfinite = true; h *= qmin; }
-      else h *= std::max(qmin, safety * std::pow(err, -expo));
+      if (!std::isfinite(err2)) { last_nonfinite = true; h *= qmin; }
+      else h *= std::max(qmin, 0.9 * std::exp(-0.5 * T.rej * std::log(err2)));
     }
   }
   return ST_OK;
@@ -474,7 +567,8 @@ struct BgSink : StepSink {
     const double h00 = 2 * s3 - 3 * s2 + 1, h10 = s3 - 2 * s2 + s, h01 = -2 * s3 + 3 * s2, h11 = s3 - s2;
     for (int i = 0; i < 5; ++i) out[i] = h00 * y0[i] + h10 * h * f0[i] + h01 * y1[i] + h11 * h * f1[i];
   }
-  bool on_step(double t0, const double* y0_, const double* f0, double t1, const double* y1, const double* f1) override {
+  bool on_step(double t0, const double* y0_, const double* f0, double t1, const double* y1, const double* f1,
+               const double*) override {
     if (y1[0] >= 1.0) {  // a = 1 event (src/solve.jl:158-203); root of the step's Hermite interpolant
       double lo = t0, hi = t1, tmp[5];
       for (int it = 0; it < 200; ++it) {
@@ -563,7 +657,7 @@ extern "C" orc_bg* orc_bg_solve(const orc_params* p, const orc_model* m, const o
   BgSys sys(P);
   BgSink sink(B->knots);
   long na, nr;
-  int st = rodas4(sys, t0, P.tau_max, y, P.rtol_bg, P.atol_bg, P.maxiters, &sink, &na, &nr);
+  int st = rosenbrock(P.alg_bg, sys, t0, P.tau_max, y, P.rtol_bg, P.atol_bg, P.maxiters, &sink, &na, &nr);
   if (!sink.hit || st != ST_OK || !std::isfinite(a)) {
     B->status = st ? st : ST_NONFINITE; *status = B->status;
     B->tau0 = B->kappa0 = B->taurec = NAN;
@@ -686,15 +780,19 @@ static void pt_psi_phidot(const Cosmo& P, const PtLayout& L, double k, const PtC
   for (int i = 0; i < n; ++i) pPhid[i] = pPhid[i] - C.Hc * pPsi[i];
 }
 
-// Dense J(tau) of the linear system u' = J(tau) u.
-template <class S>
-static void pt_jacobian(const Cosmo& P, const PtLayout& L, double k, const PtCoef<S>& C, S* J, S* pPsi, S* pPhid) {
-  const int n = L.n;
-  for (int i = 0; i < n * n; ++i) J[i] = S(0.0);
+// J(tau) of the linear system u' = J(tau) u, written through an accumulator: acc.add(r, c, v) adds
+// v to J[r][c], acc.addv(r, s, v) adds s * v (a functional's weight vector, pPsi or pPhid) to row r.
+template <class S, class Acc>
+static void pt_assemble(const Cosmo& P, const PtLayout& L, double k, const PtCoef<S>& C, Acc& acc, S* pPsi, S* pPhid) {
   pt_psi_phidot(P, L, k, C, pPsi, pPhid);
-  auto row = [&](int r) { return J + (size_t)r * n; };
-  auto addv = [&](int r, double s, const S* v) { S* R = row(r); for (int i = 0; i < n; ++i) R[i] += s * v[i]; };
-  auto addvS = [&](int r, const S& s, const S* v) { S* R = row(r); for (int i = 0; i < n; ++i) R[i] += s * v[i]; };
+  struct RowRef {
+    Acc& a; int r;
+    struct Cell { Acc& a; int r, c; void operator+=(const S& v) { a.add(r, c, v); } };
+    Cell operator[](int c) { return Cell{a, r, c}; }
+  };
+  auto row = [&](int r) { return RowRef{acc, r}; };
+  auto addv = [&](int r, double s, const S* v) { acc.addv(r, S(s), v); };
+  auto addvS = [&](int r, const S& s, const S* v) { acc.addv(r, s, v); };
   const S kd = C.kd, Hc = C.Hc;
   // metric
   addv(L.Phi, 1.0, pPhid);
@@ -712,7 +810,7 @@ static void pt_jacobian(const Cosmo& P, const PtLayout& L, double k, const PtCoe
   row(L.F(1))[L.F(0)] += k / 3; row(L.F(1))[L.F(2)] += -2 * k / 3; addv(L.F(1), 4 * k / 3, pPsi);
   row(L.F(1))[L.tb] += -(4.0 / 3.0) * kd / k; row(L.F(1))[L.F(1)] += kd;
   for (int l = 2; l < Lg; ++l) {
-    S* Rw = row(L.F(l));
+    auto Rw = row(L.F(l));
     Rw[L.F(l - 1)] += k * l / (2.0 * l + 1); Rw[L.F(l + 1)] += -k * (l + 1) / (2.0 * l + 1); Rw[L.F(l)] += kd;
     if (l == 2) { Rw[L.F(2)] += -kd / 10; Rw[L.G(0)] += -kd / 10; Rw[L.G(2)] += -kd / 10; }
   }
@@ -721,18 +819,18 @@ static void pt_jacobian(const Cosmo& P, const PtLayout& L, double k, const PtCoe
   row(L.G(0))[L.F(2)] += -kd / 2; row(L.G(0))[L.G(0)] += -kd / 2; row(L.G(0))[L.G(2)] += -kd / 2;
   row(L.G(1))[L.G(0)] += k / 3; row(L.G(1))[L.G(2)] += -2 * k / 3; row(L.G(1))[L.G(1)] += kd;
   for (int l = 2; l < Lg; ++l) {
-    S* Rw = row(L.G(l));
+    auto Rw = row(L.G(l));
     Rw[L.G(l - 1)] += k * l / (2.0 * l + 1); Rw[L.G(l + 1)] += -k * (l + 1) / (2.0 * l + 1); Rw[L.G(l)] += kd;
     if (l == 2) { Rw[L.F(2)] += -kd / 10; Rw[L.G(0)] += -kd / 10; Rw[L.G(2)] += -kd / 10; }
   }
   row(L.G(Lg))[L.G(Lg - 1)] += k; row(L.G(Lg))[L.G(Lg)] += -(Lg + 1) / C.tau + kd;
-  // massless neutrinos (src/models/neutrinos.jl:217-227)
+  // massless neutrinos (src/models/neutrinos.jl:22-26)
   const int Ln = P.Ln;
   row(L.N(0))[L.N(1)] += -k; addv(L.N(0), 4.0, pPhid);
   row(L.N(1))[L.N(0)] += k / 3; row(L.N(1))[L.N(2)] += -2 * k / 3; addv(L.N(1), 4 * k / 3, pPsi);
-  for (int l = 2; l < Ln; ++l) { S* Rw = row(L.N(l)); Rw[L.N(l - 1)] += k * l / (2.0 * l + 1); Rw[L.N(l + 1)] += -k * (l + 1) / (2.0 * l + 1); }
+  for (int l = 2; l < Ln; ++l) { auto Rw = row(L.N(l)); Rw[L.N(l - 1)] += k * l / (2.0 * l + 1); Rw[L.N(l + 1)] += -k * (l + 1) / (2.0 * l + 1); }
   row(L.N(Ln))[L.N(Ln - 1)] += k; row(L.N(Ln))[L.N(Ln)] += -(Ln + 1) / C.tau;
-  // massive neutrinos (src/models/neutrinos.jl:324-327)
+  // massive neutrinos (src/models/neutrinos.jl:129-132)
   const int Lh = P.Lh;
   for (int i = 0; i < P.nx; ++i) {
     const S E = sqrt(P.xq[i] * P.xq[i] + (P.y0 * P.y0) * (C.a * C.a));
@@ -742,11 +840,26 @@ static void pt_jacobian(const Cosmo& P, const PtLayout& L, double k, const PtCoe
     row(L.H(i, 1))[L.H(i, 0)] += (k / 3) * q; row(L.H(i, 1))[L.H(i, 2)] += -(2 * k / 3) * q;
     addvS(L.H(i, 1), -(k / 3) * dl / q, pPsi);
     for (int l = 2; l < Lh; ++l) {
-      S* Rw = row(L.H(i, l));
+      auto Rw = row(L.H(i, l));
       Rw[L.H(i, l - 1)] += k * q * (l / (2.0 * l + 1)); Rw[L.H(i, l + 1)] += -k * q * ((l + 1) / (2.0 * l + 1));
     }
     row(L.H(i, Lh))[L.H(i, Lh - 1)] += k * q; row(L.H(i, Lh))[L.H(i, Lh)] += -(Lh + 1) / C.tau;
   }
+}
+
+template <class S> struct DenseAcc {
+  S* J; int n;
+  void add(int r, int c, const S& v) { J[(size_t)r * n + c] += v; }
+  void addv(int r, const S& s, const S* v) { S* R = J + (size_t)r * n; for (int i = 0; i < n; ++i) R[i] += s * v[i]; }
+};
+
+// Dense J(tau) (the checker's form).
+template <class S>
+static void pt_jacobian(const Cosmo& P, const PtLayout& L, double k, const PtCoef<S>& C, S* J, S* pPsi, S* pPhid) {
+  const int n = L.n;
+  for (int i = 0; i < n * n; ++i) J[i] = S(0.0);
+  DenseAcc<S> acc{J, n};
+  pt_assemble<S>(P, L, k, C, acc, pPsi, pPhid);
 }
 
 // background coefficients from the spline (values, plus d/dtau through the spline for Jet<1>)
@@ -771,6 +884,16 @@ struct PtSys : OdeSys {
     pt_jacobian<double>(P, L, k, C, Jd.data(), pPsi.data(), pPhid.data());
     for (int i = 0; i < n; ++i) { double s = 0; const double* R = &Jd[(size_t)i * n]; for (int j = 0; j < n; ++j) s += R[j] * y[j]; f[i] = s; }
   }
+  // f = J y and g = J' y + J f with the coefficients C (value and τ-derivative); fills pPsij
+  virtual void source_products(const PtCoef<Jet<1>>& C, const double* y, double* f, double* g) {
+    pt_jacobian<Jet<1>>(P, L, k, C, Jj.data(), pPsij.data(), pPhidj.data());
+    for (int i = 0; i < n; ++i) { double s = 0; for (int j = 0; j < n; ++j) s += Jj[(size_t)i * n + j].c[0] * y[j]; f[i] = s; }
+    for (int i = 0; i < n; ++i) {
+      double s = 0;
+      for (int j = 0; j < n; ++j) s += Jj[(size_t)i * n + j].c[1] * y[j] + Jj[(size_t)i * n + j].c[0] * f[j];
+      g[i] = s;
+    }
+  }
   void jac(double t, const double* y, double* J, double* ft) override {
     PtCoef<Jet<1>> C; pt_coef_spline<Jet<1>>(B, t, C);
     pt_jacobian<Jet<1>>(P, L, k, C, Jj.data(), pPsij.data(), pPhidj.data());
@@ -782,8 +905,185 @@ struct PtSys : OdeSys {
   }
 };
 
-// adiabatic initial conditions (src/models/cosmologies.jl:74-77, photons.jl:169-189,
-// neutrinos.jl:228-234,329-334, generic_species.jl:54-57); Phi from the shear constraint.
+// ------------------------------------------------------------------------------------------
+// Sparse linear algebra of the CPU baseline (the reference's path: Rodas5P with a sparse LU of
+// W = I/(hγ) - J, KLU in LinearSolve.jl, src/solve.jl:314-317,327-341).  The dense PtSys above is
+// the checker; this one does the same arithmetic on the structural nonzeros only:
+//   * J is assembled into its nonzero slots (pattern found once per model from the dense form at
+//     generic times) and applied as a sparse product;
+//   * W is permuted symmetrically by a minimum-degree order of its pattern and factored by
+//     right-looking elimination with threshold partial pivoting (the diagonal is kept while it is at
+//     least a tenth of the column's largest entry), visiting only nonzero multipliers and the pivot
+//     row's nonzeros; the solves use the recorded L columns and U rows.
+struct SparsePattern {
+  int n = 0;
+  std::vector<int> slot;         // n*n -> index of the nonzero, or -1
+  std::vector<int> row, col;     // per nonzero
+  std::vector<int> fidx;         // components carrying a Ψ or Φ̇ weight
+  std::vector<int> perm, iperm;  // elimination order: position p holds component perm[p]
+};
+
+static void build_sparse_pattern(const orc_bg& B, SparsePattern& SP) {
+  const Cosmo& P = B.P; PtLayout L(P);
+  const int n = L.n;
+  SP.n = n;
+  std::vector<char> nz((size_t)n * n, 0), fz(n, 0);
+  std::vector<double> J((size_t)n * n), pPsi(n), pPhid(n);
+  const double t0 = B.knots.front().t, t1 = B.tau0;
+  const double ts[3] = {t0 * 1.37, std::sqrt(t0 * t1) * 0.91, t1 * 0.73};
+  for (double k : {1.37, 171.3}) {
+    for (double tau : ts) {
+      PtCoef<double> C; pt_coef_spline<double>(B, tau, C);
+      pt_jacobian<double>(P, L, k, C, J.data(), pPsi.data(), pPhid.data());
+      for (size_t e = 0; e < J.size(); ++e) if (J[e] != 0) nz[e] = 1;
+      for (int i = 0; i < n; ++i) if (pPsi[i] != 0 || pPhid[i] != 0) fz[i] = 1;
+    }
+  }
+  for (int i = 0; i < n; ++i) nz[(size_t)i * n + i] = 1;  // W's diagonal
+  SP.slot.assign((size_t)n * n, -1);
+  SP.row.clear(); SP.col.clear(); SP.fidx.clear();
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c)
+      if (nz[(size_t)r * n + c]) { SP.slot[(size_t)r * n + c] = (int)SP.row.size(); SP.row.push_back(r); SP.col.push_back(c); }
+  for (int i = 0; i < n; ++i) if (fz[i]) SP.fidx.push_back(i);
+  // rows that take a functional get every functional column (the assembly adds the whole vector)
+  // minimum-degree order on the symmetrised pattern
+  std::vector<std::vector<char>> adj(n, std::vector<char>(n, 0));
+  for (size_t e = 0; e < SP.row.size(); ++e) {
+    const int r = SP.row[e], c = SP.col[e];
+    if (r != c) { adj[r][c] = 1; adj[c][r] = 1; }
+  }
+  std::vector<char> done(n, 0);
+  SP.perm.clear();
+  for (int step = 0; step < n; ++step) {
+    int best = -1, bdeg = 1 << 30;
+    for (int v = 0; v < n; ++v) {
+      if (done[v]) continue;
+      int d = 0; for (int u = 0; u < n; ++u) d += (!done[u] && adj[v][u]);
+      if (d < bdeg) { bdeg = d; best = v; }
+    }
+    done[best] = 1; SP.perm.push_back(best);
+    std::vector<int> nb;
+    for (int u = 0; u < n; ++u) if (!done[u] && adj[best][u]) nb.push_back(u);
+    for (int a : nb) for (int b : nb) if (a != b) adj[a][b] = 1;
+  }
+  SP.iperm.assign(n, 0);
+  for (int p = 0; p < n; ++p) SP.iperm[SP.perm[p]] = p;
+}
+
+template <class S> struct SparseAcc {
+  const SparsePattern& P; S* v;
+  void add(int r, int c, const S& x) { v[P.slot[(size_t)r * P.n + c]] += x; }
+  void addv(int r, const S& s, const S* w) {
+    for (int i : P.fidx) { const int sl = P.slot[(size_t)r * P.n + i]; if (sl >= 0) v[sl] += s * w[i]; }
+  }
+};
+
+struct SparsePtSys : PtSys {
+  const SparsePattern& SP;
+  std::vector<double> vals, A, dinv;
+  std::vector<Jet<1>> jvals;
+  std::vector<int> piv, touched, lptr, lidx, uptr, uidx;
+  std::vector<double> lval, uval, work;
+  std::vector<char> mark;
+  SparsePtSys(const orc_bg& B_, double k_, const SparsePattern& sp) : PtSys(B_, k_), SP(sp) {
+    const size_t nnz = SP.row.size();
+    vals.resize(nnz); jvals.resize(nnz); A.assign((size_t)n * n, 0.0); dinv.resize(n); piv.resize(n); work.resize(n);
+    mark.assign((size_t)n * n, 0);
+  }
+  void rhs(double t, const double* y, double* f) override {
+    PtCoef<double> C; pt_coef_spline<double>(B, t, C);
+    std::fill(vals.begin(), vals.end(), 0.0);
+    SparseAcc<double> acc{SP, vals.data()};
+    pt_assemble<double>(P, L, k, C, acc, pPsi.data(), pPhid.data());
+    for (int i = 0; i < n; ++i) f[i] = 0;
+    for (size_t e = 0; e < vals.size(); ++e) f[SP.row[e]] += vals[e] * y[SP.col[e]];
+  }
+  bool w_factor(double t, const double* y, double ihg, double* ft) override {
+    PtCoef<Jet<1>> C; pt_coef_spline<Jet<1>>(B, t, C);
+    std::fill(jvals.begin(), jvals.end(), Jet<1>(0.0));
+    SparseAcc<Jet<1>> acc{SP, jvals.data()};
+    pt_assemble<Jet<1>>(P, L, k, C, acc, pPsij.data(), pPhidj.data());
+    for (int i = 0; i < n; ++i) ft[i] = 0;
+    for (size_t e = 0; e < jvals.size(); ++e) ft[SP.row[e]] += jvals[e].c[1] * y[SP.col[e]];
+    // W in elimination order; clear what the previous factorisation left (pattern + fill)
+    for (int p : touched) { A[p] = 0.0; mark[p] = 0; }
+    touched.clear();
+    for (size_t e = 0; e < jvals.size(); ++e) {
+      const int p = SP.iperm[SP.row[e]] * n + SP.iperm[SP.col[e]];
+      A[p] -= jvals[e].c[0];
+      if (!mark[p]) { mark[p] = 1; touched.push_back(p); }
+    }
+    for (int i = 0; i < n; ++i) { const int p = i * n + i; A[p] += ihg; if (!mark[p]) { mark[p] = 1; touched.push_back(p); } }
+    lptr.assign(1, 0); uptr.assign(1, 0); lidx.clear(); lval.clear(); uidx.clear(); uval.clear();
+    std::vector<int> rows, ucols;
+    for (int kk = 0; kk < n; ++kk) {
+      // nonzero rows of column kk at or below the diagonal
+      rows.clear();
+      double mx = 0; int pbest = -1;
+      for (int i = kk; i < n; ++i) {
+        const double a = A[i * n + kk];
+        if (a != 0) { rows.push_back(i); if (std::fabs(a) > mx) { mx = std::fabs(a); pbest = i; } }
+      }
+      if (!(mx > 0) || !std::isfinite(mx)) return false;
+      int p = kk;
+      if (!(std::fabs(A[kk * n + kk]) >= 0.1 * mx)) p = pbest;
+      piv[kk] = p;
+      if (p != kk) {
+        for (int j = 0; j < n; ++j) {
+          std::swap(A[kk * n + j], A[p * n + j]);
+          for (int q : {kk * n + j, p * n + j}) if (!mark[q]) { mark[q] = 1; touched.push_back(q); }
+        }
+        for (int& r : rows) if (r == p) r = kk; else if (r == kk) r = p;
+      }
+      const double d = 1.0 / A[kk * n + kk];
+      dinv[kk] = d;
+      ucols.clear();
+      for (int j = kk + 1; j < n; ++j) if (A[kk * n + j] != 0) { ucols.push_back(j); uidx.push_back(j); uval.push_back(A[kk * n + j]); }
+      uptr.push_back((int)uidx.size());
+      for (int i : rows) {
+        if (i == kk) continue;
+        const double l = A[i * n + kk] * d;
+        lidx.push_back(i); lval.push_back(l);
+        double* Ri = &A[i * n];
+        const double* Rk = &A[kk * n];
+        for (int j : ucols) {
+          const int q = i * n + j;
+          Ri[j] -= l * Rk[j];
+          if (!mark[q]) { mark[q] = 1; touched.push_back(q); }
+        }
+      }
+      lptr.push_back((int)lidx.size());
+    }
+    return true;
+  }
+  void source_products(const PtCoef<Jet<1>>& C, const double* y, double* f, double* g) override {
+    std::vector<Jet<1>> sv(jvals.size(), Jet<1>(0.0));
+    SparseAcc<Jet<1>> acc{SP, sv.data()};
+    pt_assemble<Jet<1>>(P, L, k, C, acc, pPsij.data(), pPhidj.data());
+    for (int i = 0; i < n; ++i) { f[i] = 0; g[i] = 0; }
+    for (size_t e = 0; e < sv.size(); ++e) f[SP.row[e]] += sv[e].c[0] * y[SP.col[e]];
+    for (size_t e = 0; e < sv.size(); ++e) g[SP.row[e]] += sv[e].c[1] * y[SP.col[e]] + sv[e].c[0] * f[SP.col[e]];
+  }
+  void w_solve(double* b) override {
+    double* x = work.data();
+    for (int i = 0; i < n; ++i) x[SP.iperm[i]] = b[i];
+    for (int kk = 0; kk < n; ++kk) {
+      if (piv[kk] != kk) std::swap(x[kk], x[piv[kk]]);
+      const double xk = x[kk];
+      for (int e = lptr[kk]; e < lptr[kk + 1]; ++e) x[lidx[e]] -= lval[e] * xk;
+    }
+    for (int kk = n - 1; kk >= 0; --kk) {
+      double v = x[kk];
+      for (int e = uptr[kk]; e < uptr[kk + 1]; ++e) v -= uval[e] * x[uidx[e]];
+      x[kk] = v * dinv[kk];
+    }
+    for (int i = 0; i < n; ++i) b[i] = x[SP.iperm[i]];
+  }
+};
+
+// adiabatic initial conditions (src/models/cosmologies.jl:74-77, photons.jl:47-67,
+// neutrinos.jl:33-39,134-139, generic_species.jl:54-57); Phi from the shear constraint.
 static void pt_initial(const orc_bg& B, double k, double tau, double* y, double* extra) {
   const Cosmo& P = B.P; PtLayout L(P);
   const int n = L.n;
@@ -832,14 +1132,20 @@ struct PtSink : StepSink {
   std::vector<double> yi;
   PtSink(PtSys& s, int nt, const double* ts, int md, double* o) : S(s), ntau(nt), taus(ts), mode(md), out(o) { yi.resize(s.n); }
   void emit(int it, double tau, const double* y);
-  bool on_step(double t0, const double* y0, const double* f0, double t1, const double* y1, const double* f1) override {
+  bool on_step(double t0, const double* y0, const double* f0, double t1, const double* y1, const double* f1,
+               const double* K) override {
     const int n = S.n;
     while (next < ntau && taus[next] <= t1) {
       const double tau = taus[next];
       if (tau < t0) { emit(next, tau, nullptr); ++next; continue; }
       const double h = t1 - t0, s = (tau - t0) / h, s2 = s * s, s3 = s2 * s;
-      const double h00 = 2 * s3 - 3 * s2 + 1, h10 = s3 - 2 * s2 + s, h01 = -2 * s3 + 3 * s2, h11 = s3 - s2;
-      for (int i = 0; i < n; ++i) yi[i] = h00 * y0[i] + h10 * h * f0[i] + h01 * y1[i] + h11 * h * f1[i];
+      if (K) {
+        const double s1 = 1 - s;
+        for (int i = 0; i < n; ++i) yi[i] = s1 * y0[i] + s * (y1[i] + s1 * (K[i] + s * (K[n + i] + s * K[2 * n + i])));
+      } else {
+        const double h00 = 2 * s3 - 3 * s2 + 1, h10 = s3 - 2 * s2 + s, h01 = -2 * s3 + 3 * s2, h11 = s3 - s2;
+        for (int i = 0; i < n; ++i) yi[i] = h00 * y0[i] + h10 * h * f0[i] + h01 * y1[i] + h11 * h * f1[i];
+      }
       emit(next, tau, yi.data());
       ++next;
     }
@@ -859,11 +1165,9 @@ static void pt_sources(PtSys& S, double tau, const double* y, double* src) {
   PtCoef<Jet<1>> C;
   auto t1 = [](const Jet<3>& x) { Jet<1> r; r.c[0] = x.c[0]; r.c[1] = x.c[1]; return r; };
   C.a = t1(o.a); C.Hc = t1(o.Hc); C.kd = t1(o.kd); C.cs2 = t1(o.cs2); C.tau = Jet<1>::var(tau);
-  std::vector<Jet<1>> J((size_t)n * n), pPsi(n), pPhid(n);
-  pt_jacobian<Jet<1>>(P, L, k, C, J.data(), pPsi.data(), pPhid.data());
   std::vector<double> f(n), g(n);
-  for (int i = 0; i < n; ++i) { double s = 0; for (int j = 0; j < n; ++j) s += J[(size_t)i * n + j].c[0] * y[j]; f[i] = s; }
-  for (int i = 0; i < n; ++i) { double s = 0; for (int j = 0; j < n; ++j) s += J[(size_t)i * n + j].c[1] * y[j] + J[(size_t)i * n + j].c[0] * f[j]; g[i] = s; }
+  S.source_products(C, y, f.data(), g.data());  // f = J y, g = J' y + J f; S.pPsij holds Ψ's weights
+  const std::vector<Jet<1>>& pPsi = S.pPsij;
   double Psi = 0, Psid = 0;
   for (int i = 0; i < n; ++i) { Psi += pPsi[i].c[0] * y[i]; Psid += pPsi[i].c[1] * y[i] + pPsi[i].c[0] * f[i]; }
   const double Phi = y[L.Phi], Phid = f[L.Phi];
@@ -935,10 +1239,15 @@ extern "C" int orc_pt_solve(const orc_bg* b, int nk, const double* ks, const dou
   const orc_bg& B = *b;
   const int n = PtLayout(B.P).n;
   const double tstart = B.knots.front().t, tend = B.tau0;
+  SparsePattern SP;
+  const bool sparse = B.P.pt_linsolve == ORC_LINSOLVE_SPARSE;
+  if (sparse) build_sparse_pattern(B, SP);
 #pragma omp parallel for schedule(dynamic, 1)
   for (int ik = 0; ik < nk; ++ik) {
     const double k = ks[ik];
-    PtSys sys(B, k);
+    PtSys dense_sys(B, k);
+    SparsePtSys* sp = sparse ? new SparsePtSys(B, k, SP) : nullptr;
+    PtSys& sys = sp ? *sp : dense_sys;
     double ti = std::min(std::max(tau_ini[ik], tstart), tend);
     std::vector<double> y(n);
     pt_initial(B, k, ti, y.data(), nullptr);
@@ -949,13 +1258,14 @@ extern "C" int orc_pt_solve(const orc_bg* b, int nk, const double* ks, const dou
     // output points at the initial time
     while (mode != 1 && sink.next < ntau && taus[sink.next] <= ti) { sink.emit(sink.next, taus[sink.next], taus[sink.next] < ti ? nullptr : y.data()); ++sink.next; }
     long na = 0, nr = 0;
-    int st = rodas4(sys, ti, tend, y.data(), B.P.rtol_pt, B.P.atol_pt, B.P.maxiters, &sink, &na, &nr);
+    int st = rosenbrock(B.P.alg_pt, sys, ti, tend, y.data(), B.P.rtol_pt, B.P.atol_pt, B.P.maxiters, &sink, &na, &nr);
     if (mode != 1) while (sink.next < ntau) { sink.emit(sink.next, taus[sink.next], nullptr); ++sink.next; }
     bool finite = true; for (int i = 0; i < n; ++i) finite = finite && std::isfinite(y[i]);
     if (st == 0 && !finite) st = 3;
     if (mode == 1) out[ik] = pt_delta_m(B, k, tend, y.data());
     if (status) status[ik] = st;
     if (stats) { stats[2 * ik] = na; stats[2 * ik + 1] = nr; }
+    delete sp;
   }
   return 0;
 }

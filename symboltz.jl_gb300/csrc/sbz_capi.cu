@@ -901,25 +901,28 @@ int sbz_cl_integrate(int nk, const double* ks, const double* P0, int nl, const d
     invden[i] = 1.0 / den;
     cprime[i] = h1 * invden[i];
   }
-  double *d_ks, *d_P0, *d_A, *d_B, *d_c, *d_i, *d_z, *d_Cl;
+  // every buffer is released on every return path, the early error returns included
+  struct Owned : DevBuf {
+    ~Owned() { release(); }
+  } d_ks, d_P0, d_A, d_B, d_c, d_i, d_z, d_Cl;
   const size_t th = sizeof(double) * (size_t)nk * nl;
-  SBZ_CUDA(cudaMalloc(&d_ks, sizeof(double) * nk));
-  SBZ_CUDA(cudaMalloc(&d_P0, sizeof(double) * nk));
-  SBZ_CUDA(cudaMalloc(&d_A, th));
-  SBZ_CUDA(cudaMalloc(&d_B, th));
-  SBZ_CUDA(cudaMalloc(&d_c, sizeof(double) * np));
-  SBZ_CUDA(cudaMalloc(&d_i, sizeof(double) * np));
-  SBZ_CUDA(cudaMalloc(&d_z, sizeof(double) * (size_t)np * nl));
-  SBZ_CUDA(cudaMalloc(&d_Cl, sizeof(double) * nl));
-  SBZ_CUDA(cudaMemcpy(d_ks, ks, sizeof(double) * nk, cudaMemcpyHostToDevice));
-  SBZ_CUDA(cudaMemcpy(d_P0, P0, sizeof(double) * nk, cudaMemcpyHostToDevice));
-  SBZ_CUDA(cudaMemcpy(d_A, ThA, th, cudaMemcpyHostToDevice));
-  SBZ_CUDA(cudaMemcpy(d_B, ThB, th, cudaMemcpyHostToDevice));
-  SBZ_CUDA(cudaMemcpy(d_c, cprime.data(), sizeof(double) * np, cudaMemcpyHostToDevice));
-  SBZ_CUDA(cudaMemcpy(d_i, invden.data(), sizeof(double) * np, cudaMemcpyHostToDevice));
-  int r = sbz::cl_launch(nk, d_ks, d_P0, nl, d_A, d_B, d_c, d_i, d_z, d_Cl, 0);
-  if (r == 0) SBZ_CUDA(cudaMemcpy(Cl, d_Cl, sizeof(double) * nl, cudaMemcpyDeviceToHost));
-  for (double* p : {d_ks, d_P0, d_A, d_B, d_c, d_i, d_z, d_Cl}) cudaFree(p);
+  SBZ_CUDA(d_ks.ensure(sizeof(double) * nk));
+  SBZ_CUDA(d_P0.ensure(sizeof(double) * nk));
+  SBZ_CUDA(d_A.ensure(th));
+  SBZ_CUDA(d_B.ensure(th));
+  SBZ_CUDA(d_c.ensure(sizeof(double) * np));
+  SBZ_CUDA(d_i.ensure(sizeof(double) * np));
+  SBZ_CUDA(d_z.ensure(sizeof(double) * (size_t)np * nl));
+  SBZ_CUDA(d_Cl.ensure(sizeof(double) * nl));
+  SBZ_CUDA(cudaMemcpy(d_ks.p, ks, sizeof(double) * nk, cudaMemcpyHostToDevice));
+  SBZ_CUDA(cudaMemcpy(d_P0.p, P0, sizeof(double) * nk, cudaMemcpyHostToDevice));
+  SBZ_CUDA(cudaMemcpy(d_A.p, ThA, th, cudaMemcpyHostToDevice));
+  SBZ_CUDA(cudaMemcpy(d_B.p, ThB, th, cudaMemcpyHostToDevice));
+  SBZ_CUDA(cudaMemcpy(d_c.p, cprime.data(), sizeof(double) * np, cudaMemcpyHostToDevice));
+  SBZ_CUDA(cudaMemcpy(d_i.p, invden.data(), sizeof(double) * np, cudaMemcpyHostToDevice));
+  int r = sbz::cl_launch(nk, d_ks.as<double>(), d_P0.as<double>(), nl, d_A.as<double>(), d_B.as<double>(), d_c.as<double>(),
+                         d_i.as<double>(), d_z.as<double>(), d_Cl.as<double>(), 0);
+  if (r == 0) SBZ_CUDA(cudaMemcpy(Cl, d_Cl.p, sizeof(double) * nl, cudaMemcpyDeviceToHost));
   return r == 0 ? SBZ_OK : fail(SBZ_ERR_CUDA, "C_l kernel");
 }
 

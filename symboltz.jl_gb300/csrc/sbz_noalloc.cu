@@ -13,11 +13,12 @@
 //  * Every call shares the one array per device and it keeps the previous call's contents, so two
 //    calls whose kernels overlap on the GPU (different streams, or different host threads) race.
 //    Calls issued on one stream run one after the other and are safe.
-//  * The first call on a device looks up the array's device address (cudaGetSymbolAddress, which
-//    loads this module on that device); make that first call before any stream capture.
+//  * Every call looks up the array's device address on the current device and context
+//    (cudaGetSymbolAddress; no address is cached, so a reset device or another context gets its own
+//    copy).  The first call on a device also loads this module there; make that first call before
+//    any stream capture.
 #include <cuda_runtime.h>
 #include <cstdio>
-#include <mutex>
 #include "../../include/symboltz_gb300.h"
 #include "sbz_los.cuh"
 
@@ -30,10 +31,6 @@ namespace {
 // File-scope scratch.  On the host `g_scratch` is only a stand-in symbol: its device address is
 // obtained per device with cudaGetSymbolAddress and passed to the kernels as a plain pointer.
 static __device__ __align__(256) double g_scratch[SBZ_NOALLOC_SCRATCH_DOUBLES];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-double* g_dev_scratch[kMaxDevices] = {};
 
 // scratch layout (offsets in doubles, each region 256-byte aligned): cprime[np] | invden[np] | z[np*nl]
 inline long long pad32(long long n) { return (n + 31) / 32 * 32; }
@@ -66,18 +63,15 @@ __global__ void noalloc_factors_kernel(int nk, const double* __restrict__ ks, do
   }
 }
 
+// Device address of the scratch in the current device's current context, looked up on every call:
+// after a device reset, or in a context other than the primary one, an address kept from an earlier
+// call would point at memory that is no longer this module's.
 double* scratch_for_current_device(int* err) {
   int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) { *err = 1; return nullptr; }
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_dev_scratch[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_scratch);
-    if (e != cudaSuccess || !p) { *err = 2; return nullptr; }
-    g_dev_scratch[dev] = static_cast<double*>(p);
-  }
-  return g_dev_scratch[dev];
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) { *err = 1; return nullptr; }
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) { *err = 2; return nullptr; }
+  return static_cast<double*>(p);
 }
 
 }  // namespace

@@ -3,8 +3,8 @@
 // Follows the reference's component equations:
 //   constants                     src/constants.jl:3-50 (CODATA 2018, IAU parsec, atomic masses)
 //   Friedmann equation            src/models/gravity.jl:31
-//   species densities             src/models/generic_species.jl:30-32, photons.jl:166-168,
-//                                 neutrinos.jl:273-313, cosmologies.jl:78-84,221-227
+//   species densities             src/models/generic_species.jl:30-32, photons.jl:44-46,
+//                                 neutrinos.jl:78-86,109-118, cosmologies.jl:78-84,221-227
 //   baryon thermodynamics         src/models/baryons.jl:145-212
 //   RECFAST 1.5.2 recombination   src/models/baryons.jl:14-116 (Hswitch 0/1, Heswitch 0/6)
 //   tanh reionization             src/models/baryons.jl:128-138,201-205

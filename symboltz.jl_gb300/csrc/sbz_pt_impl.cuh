@@ -3,18 +3,18 @@
 // a group of NW warps integrates one (cosmology, k) mode.
 //
 // Replaces the per-k loop of solvept (src/solve.jl:543-569) and the Rodas5P + KLU inner solver
-// it calls (src/solve.jl:327-341).  Integrator: Hairer-Wanner RODAS (Rosenbrock, order 4(3),
-// stiffly accurate) in transformed form
+// it calls (src/solve.jl:327-341).  Integrator: Rodas5P (Rosenbrock, order 5(4), stiffly
+// accurate; tableau in sbz_rosenbrock.cuh) in transformed form
 //   (1/(hγ) - J) U_i = f(t+c_i h, y + Σ A_ij U_j) + Σ (C_ij/h) U_j + h d_i ∂f/∂τ,
-//   y1 = y + Σ A_5j U_j + U_5 + U_6, error estimate U_6,
-// with the error norm, PI step-size control and Hermite dense output of OrdinaryDiffEq-style
-// integrators.  The perturbation system is linear, u' = J(τ) u, so "f" and "J·x" are one
-// operator; its rows are described in sbz_layout.hpp.
+//   y1 = y + Σ_{j<8} A_8j U_j + U_8, error estimate U_8,
+// with the error norm, PI step-size control and an order-4 continuous extension for the saved
+// times.  The perturbation system is linear, u' = J(τ) u, so "f" and "J·x" are one operator; its
+// rows are described in sbz_layout.hpp.
 //
 // Stage solves exploit the structure of M = 1/(hγ) - B (J = B + c_Φ̇ ∇Φ̇ᵀ + c_Ψ ∇Ψᵀ):
-//   * the free-streaming hierarchies are tridiagonal chains, eliminated from their truncation
-//     end by one thread each (all chains in parallel, no pivoting needed: pivots stay ≥ 1/(hγ));
-//   * photon-baryon rows δb, θb, F0-2, G0-2 form a dense 8x8 head (LU with partial pivoting);
+//   * the free-streaming hierarchies are tridiagonal chains, eliminated from their truncation end
+//     by warp scans (no pivoting needed: pivots stay ≥ 1/(hγ));
+//   * photon-baryon rows δb, θb, F0-2, G0-2 form a dense 8x8 head (explicit inverse, partial pivoting);
 //   * CDM and Φ are 2x2/1x1 triangular blocks;
 //   * the two metric couplings are added back with a rank-2 Sherman-Morrison-Woodbury update.
 // ST = double: all-FP64 solve.  ST = float: FP32 factorisation and solves with FP64 iterative
@@ -32,28 +32,18 @@
 #include <cstdint>
 #include "sbz_layout.hpp"
 #include "sbz_pt.cuh"
+#include "sbz_rosenbrock.cuh"
 
 namespace sbz {
 namespace ptk {
 
 constexpr unsigned FULL = 0xffffffffu;
 
-namespace rw {
-constexpr double gam = 0.25;
-constexpr double c2 = 0.386, c3 = 0.21, c4 = 0.63;
-constexpr double d1 = 0.25, d2 = -0.1043, d3 = 0.1035, d4 = -0.0362;
-constexpr double A21 = 1.544, A31 = 0.9466785280815826, A32 = 0.2557011698983284;
-constexpr double A41 = 3.314825187068521, A42 = 2.896124015972201, A43 = 0.9986419139977817;
-constexpr double A51 = 1.221224509226641, A52 = 6.019134481288629, A53 = 12.53708332932087, A54 = -0.6878860361058950;
-constexpr double C21 = -5.6688, C31 = -2.430093356833875, C32 = -0.2063599157091915;
-constexpr double C41 = -0.1073529058151375, C42 = -9.594562251023355, C43 = -20.47028614809616;
-constexpr double C51 = 7.496443313967647, C52 = -10.24680431464352, C53 = -33.99990352819905, C54 = 11.70890893206160;
-constexpr double C61 = 8.083246795921522, C62 = -7.981132988064893, C63 = -31.52159432874371, C64 = 16.31930543123136, C65 = -6.058818238834054;
-}  // namespace rw
+using TB = ros::Rodas5P;  // the integrator's tableau
 
 constexpr int kWF = 2 * kMaxFun;  // functional weights per set: Ψ terms then δρ terms
-constexpr int kMaxT = 4;          // coefficient sets evaluated in one pass (the four stage times)
-constexpr int kNSets = 6;         // J (step start), three stage times, step end, output time
+constexpr int kMaxT = TB::NTIME;  // coefficient sets evaluated in one call (the later stage times)
+constexpr int kNSets = TB::NTIME + 2;  // J (step start), the later stage times (the last is the step end), output time
 
 static_assert(sizeof(ModelDesc) % 4 == 0 && sizeof(CompDesc) % 4 == 0 && sizeof(CosmoDesc) % 4 == 0, "word copies");
 
@@ -212,8 +202,8 @@ __device__ __forceinline__ void table_hermite(const CosmoDesc* __restrict__ cd, 
 // τ-dependent coefficients at nt ≤ kMaxT times into sets cs[set[q]]; derivative sets where bit q
 // of dmask is set.  source = true (nt = 1): also fetch e^{-κ}, κ̈, κ⃛ and use the Taylor-mode κ̈
 // as dκ̇/dτ (the line-of-sight sources differentiate the background along its ODE,
-// src/models/cosmologies.jl:99-105).  Warp 0 forms the base scalars in one pass, lane = 8 q + c:
-// lane c < 7 interpolates table quantity c at time q once; lanes c = 0, 1, 7 then share one
+// src/models/cosmologies.jl:99-105).  Warp p forms the base scalars of times 4p..4p+3, lane =
+// 8 (q - 4p) + c: lane c < 7 interpolates table quantity c at time q once; lanes c = 0, 1, 7 then share one
 // reciprocal path (1/a, 1/ℋ, 1/τ) and lanes c < nx one momentum-bin energy path (a from lane 8q by
 // shuffle), so no quantity is interpolated twice.  The expressions are then spread over the group.
 // The caller guarantees that no thread still reads the target sets; the call ends with a group
@@ -222,8 +212,9 @@ template <int NW, int NSL, typename ST>
 __device__ __forceinline__ void coef_eval(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const int* set, const double* taus, int nt,
                           unsigned dmask, bool source, const CosmoDesc* cd, const double* __restrict__ tab,
                           int nexpr, int nx, const ModeK& mk) {
-  if (g.wq == 0) {
-    const int lane = g.lane, q = lane >> 3, c = lane & 7;
+  // times 4p..4p+3 in pass p: warp p of the group, or every pass on the one warp when NW = 1
+  for (int pass = NW == 1 ? 0 : g.wq; 4 * pass < nt; pass += NW) {
+    const int lane = g.lane, q = 4 * pass + (lane >> 3), c = lane & 7;
     const bool live = q < nt;
     const bool dq = live && ((dmask >> q) & 1u);
     double v = 0, d = 0;
@@ -544,7 +535,7 @@ __device__ __forceinline__ void functionals_st(const Grp<NW>& g, const ModeMem<N
 template <int NW, int NSL, typename ST>
 __device__ __forceinline__ void factorize(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, Factor<ST>& F, const CSet& C,
                                           const CompDesc* __restrict__ comps, const ModelDesc& M, double k, double h,
-                                          double s, bool scan) {
+                                          double s, double gam, bool scan) {
   const int gt = g.gt, lane = g.lane;
   const double* cv = C.cv;
   // per-row inputs, all threads: diagonal s - (dg + tr), the two chain couplings, the rank-2
@@ -680,7 +671,7 @@ __device__ __forceinline__ void factorize(const Grp<NW>& g, ModeMem<NW, NSL, ST>
       for (int q = 0; q < 8; ++q) W.Hinv[r * 8 + q] = e[q];
     }
   }
-  F.is = (ST)(h * rw::gam);
+  F.is = (ST)(h * gam);
   F.ihc = rcp<ST>((ST)(s - cv[CV_MH]));
   g.sync();
   // rank-2 correction: Z1 = M⁻¹ c_Φ̇, Z2 = M⁻¹ c_Ψ
@@ -875,7 +866,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
     int status = SBZ_OK;
     int64_t nacc = 0, nrej = 0;
     double y[NSL], f0[NSL], ft[NSL];
-    int sJ = 0, s5 = 4;  // coefficient-set roles: J (step start) and step end swap on acceptance
+    int sJ = 0, sE = TB::NTIME;  // coefficient-set roles: J (step start) and step end swap on acceptance
     const int sIC = kNSets - 1;
 
     // ---- adiabatic initial conditions (src/models/cosmologies.jl:74-77 and species ieqs) ----
@@ -972,9 +963,9 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl] + h0 * f0[sl]; }
         const double th = t + h0;
-        coef_eval(g, W, &s5, &th, 1, 0u, false, cd, tab, M.nexpr, M.nx, mk);
+        coef_eval(g, W, &sE, &th, 1, 0u, false, cd, tab, M.nexpr, M.nx, mk);
         double f1[NSL];
-        matvec<NW, NSL>(g, W.x, W.cs[s5], comps, M, k, f1);
+        matvec<NW, NSL>(g, W.x, W.cs[sE], comps, M, k, f1);
         double d2 = 0;
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) {
@@ -987,12 +978,11 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         h = fmin(100 * h0, h1);
         if (!isfinite(h) || h <= 0) h = 1e-6 * fmax(1.0, t);
       }
-      double errold = 1e-4;   // previous accepted error norm (FP64 controller)
-      float errold2f = 1e-8f; // its square (FP32 controller)
+      constexpr double kLogErrFloor = -9.210340371976184;  // log(1e-4): the controller's floor on errold
+      double lerrold = kLogErrFloor;  // log of the previous accepted error norm
       bool rejected = false, nonfinite = false, have_jac = false;
       Factor<ST> F;
       int64_t iters = 0;
-      const int s2 = 1, s3 = 2, s4 = 3;
       while (t < tend) {
         if (++iters > A.maxiters) { status = SBZ_MAXITERS; break; }
         if (t + 1.01 * h >= tend) h = tend - t;
@@ -1006,97 +996,86 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
           matvec_dtau<NW, NSL>(g, W.x, CJ, comps, M, k, ft);
           have_jac = true;
         }
-        const double ih = 1.0 / h, s = 4.0 * ih;  // s = 1/(hγ), γ = 1/4
+        const double ih = 1.0 / h, s = 1.0 / (h * TB::gam);
         const double tn = (h == tend - t) ? tend : t + h;
+        // coefficient set of each later stage time: 1..NTIME-1 in place, the step end in sE
+        int tset[TB::NTIME + 1];
+#pragma unroll
+        for (int q = 1; q < TB::NTIME; ++q) tset[q] = q;
+        tset[TB::NTIME] = sE;
         {
-          // coefficients at the four later stage times (the last one with τ-derivatives: it is
+          // coefficients at the later stage times (the last one, t + h, with τ-derivatives: it is
           // the next step's Jacobian set), and the factorisation for this h
-          const int sets[4] = {s2, s3, s4, s5};
-          const double tt[4] = {t + rw::c2 * h, t + rw::c3 * h, t + rw::c4 * h, tn};
+          double tt[TB::NTIME];
+#pragma unroll
+          for (int q = 1; q < TB::NTIME; ++q) {
+            int st = 1;
+#pragma unroll
+            for (int i = 1; i < TB::S; ++i) if (TB::tslot(i) == q) st = i;
+            tt[q - 1] = t + TB::c(st) * h;
+          }
+          tt[TB::NTIME - 1] = tn;
           g.sync();  // the previous step's readers of these sets are done
-          coef_eval(g, W, sets, tt, 4, 8u, false, cd, tab, M.nexpr, M.nx, mk);
-          factorize(g, W, F, CJ, comps, M, k, h, s, scan);
+          coef_eval(g, W, tset + 1, tt, TB::NTIME, 1u << (TB::NTIME - 1), false, cd, tab, M.nexpr, M.nx, mk);
+          factorize(g, W, F, CJ, comps, M, k, h, s, TB::gam, scan);
         }
-        double U1[NSL], U2[NSL], U3[NSL], U4[NSL], U5[NSL], U6[NSL], b[NSL], Fv[NSL];
+        double U[TB::S][NSL], b[NSL], Fv[NSL], Y[NSL];
         float isk[NSL];  // refinement stopping weights
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) isk[sl] = 1.0f / (float)(atol + rtol * fabs(y[sl]));
 #pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) b[sl] = f0[sl] + h * rw::d1 * ft[sl];
+        for (int sl = 0; sl < NSL; ++sl) b[sl] = f0[sl] + h * TB::d(0) * ft[sl];
         float c1 = 1e30f;
-        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, isk, b, U1, &c1);
-        // lazy refinement: stages 2-6 share stage 1's W; when its first FP64 correction is already
-        // below refine_skip (error-weight units) the FP32 solves are accurate and are not refined
+        stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, isk, b, U[0], &c1);
+        // lazy refinement: the later stages share stage 1's W; when its first FP64 correction is
+        // already below refine_skip (error-weight units) the FP32 solves are accurate and are not refined
         const int rk = (A.refine > 0 && c1 < A.refine_skip) ? 0 : A.refine;
-        // stage 2
 #pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl] + rw::A21 * U1[sl]; }
-        g.sync();
-        matvec<NW, NSL>(g, W.x, W.cs[s2], comps, M, k, Fv);
-#pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + (ih * (rw::C21 * U1[sl]) + h * rw::d2 * ft[sl]);
-        stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U2);
-        // stage 3
-#pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl] + rw::A31 * U1[sl] + rw::A32 * U2[sl]; }
-        g.sync();
-        matvec<NW, NSL>(g, W.x, W.cs[s3], comps, M, k, Fv);
-#pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + (ih * (rw::C31 * U1[sl] + rw::C32 * U2[sl]) + h * rw::d3 * ft[sl]);
-        stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U3);
-        // stage 4
-#pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl] + rw::A41 * U1[sl] + rw::A42 * U2[sl] + rw::A43 * U3[sl]; }
-        g.sync();
-        matvec<NW, NSL>(g, W.x, W.cs[s4], comps, M, k, Fv);
-#pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + (ih * (rw::C41 * U1[sl] + rw::C42 * U2[sl] + rw::C43 * U3[sl]) + h * rw::d4 * ft[sl]);
-        stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U4);
-        // stage 5 (at t + h)
-        double Y[NSL];
-#pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) {
-          const int i = comp_of<NW>(gt, sl);
-          Y[sl] = y[sl] + rw::A51 * U1[sl] + rw::A52 * U2[sl] + rw::A53 * U3[sl] + rw::A54 * U4[sl];
-          if (i < n) W.x[i] = Y[sl];
-        }
-        g.sync();
-        matvec<NW, NSL>(g, W.x, W.cs[s5], comps, M, k, Fv);
-#pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C51 * U1[sl] + rw::C52 * U2[sl] + rw::C53 * U3[sl] + rw::C54 * U4[sl]);
-        stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U5);
-        // stage 6
-#pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); Y[sl] += U5[sl]; if (i < n) W.x[i] = Y[sl]; }
-        g.sync();
-        matvec<NW, NSL>(g, W.x, W.cs[s5], comps, M, k, Fv);
-#pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) b[sl] = Fv[sl] + ih * (rw::C61 * U1[sl] + rw::C62 * U2[sl] + rw::C63 * U3[sl] + rw::C64 * U4[sl] + rw::C65 * U5[sl]);
-        stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U6);
-        // error estimate and new state (the norm only steers the step size: FP32 in mixed mode)
-        double y1[NSL], err2;
-        if constexpr (sizeof(ST) == 4) {
-          float e2 = 0;
+        for (int st = 1; st < TB::S; ++st) {
+          // stage input: y + Σ A_st,j U_j, or the previous input plus U_{st-1}
 #pragma unroll
           for (int sl = 0; sl < NSL; ++sl) {
             const int i = comp_of<NW>(gt, sl);
-            y1[sl] = Y[sl] + U6[sl];
-            if (i < n) {
-              const float sk = (float)atol + (float)rtol * fmaxf(fabsf((float)y[sl]), fabsf((float)y1[sl]));
-              const float q = __fdividef((float)U6[sl], sk);
-              e2 += q * q;
+            double v;
+            if (TB::incremental(st)) {
+              v = Y[sl] + U[st - 1][sl];
+            } else {
+              v = y[sl];
+#pragma unroll
+              for (int j = 0; j < st; ++j) if (TB::A(st, j) != 0.0) v += TB::A(st, j) * U[j][sl];
             }
+            Y[sl] = v;
+            if (i < n) W.x[i] = v;
           }
-          err2 = (double)(group_sum(g, W, e2) * (float)inv_n);  // squared RMS error norm
-        } else {
+          g.sync();
+          matvec<NW, NSL>(g, W.x, W.cs[tset[TB::tslot(st)]], comps, M, k, Fv);
+#pragma unroll
+          for (int sl = 0; sl < NSL; ++sl) {
+            double cu = 0;
+#pragma unroll
+            for (int j = 0; j < st; ++j) cu += TB::C(st, j) * U[j][sl];
+            b[sl] = Fv[sl] + ih * cu;
+            if (TB::d(st) != 0.0) b[sl] += h * TB::d(st) * ft[sl];
+          }
+          stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U[st]);
+        }
+        // new state (stiffly accurate: y1 = last stage input + last stage) and the FP64 error norm
+        // of the last stage (the stage solutions are FP64 after refinement; only the
+        // factorisation was FP32)
+        double y1[NSL], err2;
+        {
           double e2 = 0;
 #pragma unroll
           for (int sl = 0; sl < NSL; ++sl) {
             const int i = comp_of<NW>(gt, sl);
-            y1[sl] = Y[sl] + U6[sl];
-            if (i < n) { const double sk = atol + rtol * fmax(fabs(y[sl]), fabs(y1[sl])); const double q = U6[sl] / sk; e2 += q * q; }
+            y1[sl] = Y[sl] + U[TB::S - 1][sl];
+            if (i < n) {
+              const double sk = atol + rtol * fmax(fabs(y[sl]), fabs(y1[sl]));
+              const double q = U[TB::S - 1][sl] / sk;
+              e2 += q * q;
+            }
           }
-          err2 = group_sum(g, W, e2) * inv_n;
+          err2 = group_sum(g, W, e2) * inv_n;  // squared RMS error norm
         }
         if (isfinite(err2) && err2 <= 1.0) {
           // accept: f(t1, y1) with the t1 coefficients, then dense output
@@ -1104,19 +1083,28 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
           for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y1[sl]; }
           g.sync();
           double f1[NSL];
-          matvec<NW, NSL>(g, W.x, W.cs[s5], comps, M, k, f1);
+          matvec<NW, NSL>(g, W.x, W.cs[sE], comps, M, k, f1);
           // the t1 coefficient set becomes the next step's Jacobian set
-          { const int tsw = sJ; sJ = s5; s5 = tsw; }
-          if (taus) {
-            bool first_out = true;
+          { const int tsw = sJ; sJ = sE; sE = tsw; }
+          if (taus && jout < A.ntau && taus[jout] <= tn) {
+            // continuous extension y(t + θh) = (1-θ) y + θ (y1 + (1-θ)(K0 + θ K1 + θ² K2))
+            double K[TB::NDENSE][NSL];
+#pragma unroll
+            for (int r = 0; r < TB::NDENSE; ++r)
+#pragma unroll
+              for (int sl = 0; sl < NSL; ++sl) {
+                double v = 0;
+#pragma unroll
+                for (int j = 0; j < TB::S; ++j) if (TB::dense(r, j) != 0.0) v += TB::dense(r, j) * U[j][sl];
+                K[r][sl] = v;
+              }
+            g.sync();  // x readers of the f1 product are done
             while (jout < A.ntau && taus[jout] <= tn) {
               const double tau = taus[jout];
-              const double hh = tn - t, sx = (tau - t) / hh, sq = sx * sx, s3x = sq * sx;
-              const double h00 = 2 * s3x - 3 * sq + 1, h10 = s3x - 2 * sq + sx, h01 = 3 * sq - 2 * s3x, h11 = s3x - sq;
+              const double th = (tau - t) / (tn - t), th1 = 1.0 - th;
               double yo[NSL];
 #pragma unroll
-              for (int sl = 0; sl < NSL; ++sl) yo[sl] = h00 * y[sl] + h10 * hh * f0[sl] + h01 * y1[sl] + h11 * hh * f1[sl];
-              if (first_out) { g.sync(); first_out = false; }  // x readers of the f1 product are done
+              for (int sl = 0; sl < NSL; ++sl) yo[sl] = th1 * y[sl] + th * (y1[sl] + th1 * (K[0][sl] + th * (K[1][sl] + th * K[2][sl])));
               emit_output(g, W, A, cd, tab, comps, M, mk, tau, yo, item, jout);
               ++jout;
             }
@@ -1125,21 +1113,14 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
 #pragma unroll
           for (int sl = 0; sl < NSL; ++sl) { y[sl] = y1[sl]; f0[sl] = f1[sl]; }
           ++nacc;
-          // PI controller fac = 0.9 err^-0.175 errold^0.1: FP32 in mixed mode (a heuristic; FP64 pow
-          // costs ~90 FP64 instructions on this GPU), FP64 as the CPU integrators otherwise
-          if constexpr (sizeof(ST) == 4) {
-            const float e2f = fmaxf((float)err2, 1e-20f);
-            float fac = 0.9f * exp2f(-0.0875f * __log2f(e2f) + 0.05f * __log2f(errold2f));
-            fac = fminf(10.0f, fmaxf(0.2f, fac));
-            if (rejected) fac = fminf(fac, 1.0f);
-            errold2f = fmaxf(e2f, 1e-8f);
-            h *= (double)fac;
-          } else {
-            const double err = sqrt(err2);
-            double fac = 0.9 * pow(fmax(err, 1e-10), -0.175) * pow(errold, 0.1);
+          // PI controller fac = 0.9 err^-beta1 errold^beta2 (OrdinaryDiffEq's defaults for the
+          // method's order), FP64 in both precisions; log(errold) is kept from the previous acceptance
+          {
+            const double lerr = 0.5 * log(fmax(err2, 1e-20));
+            double fac = 0.9 * exp(-TB::beta1 * lerr + TB::beta2 * lerrold);
             fac = fmin(10.0, fmax(0.2, fac));
             if (rejected) fac = fmin(fac, 1.0);
-            errold = fmax(err, 1e-4);
+            lerrold = fmax(lerr, kLogErrFloor);
             h *= fac;
           }
           rejected = false; nonfinite = false; have_jac = false;
@@ -1148,8 +1129,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
           ++nrej;
           rejected = true;
           if (!isfinite(err2)) { nonfinite = true; h *= 0.2; }
-          else if constexpr (sizeof(ST) == 4) h *= (double)fmaxf(0.2f, 0.9f * exp2f(-0.125f * __log2f((float)err2)));
-          else h *= fmax(0.2, 0.9 * pow(err2, -0.125));  // 0.9 err^-1/4
+          else h *= fmax(0.2, 0.9 * exp(-0.5 * TB::rej * log(err2)));
           // J's coefficients (at t) and ∂f/∂τ stay valid; only the factorisation changes
         }
       }

@@ -2,8 +2,8 @@
 // The row descriptors encode the perturbation equations of
 //   metric/GR                 src/models/gravity.jl:37-42
 //   CDM, baryons              src/models/generic_species.jl:46-47, cosmologies.jl:95
-//   photons T + P             src/models/photons.jl:151-192
-//   massless / massive ν      src/models/neutrinos.jl:217-227, 324-327
+//   photons T + P             src/models/photons.jl:28-60
+//   massless / massive ν      src/models/neutrinos.jl:22-26, 129-132
 // in the generic row form documented in sbz_layout.hpp.
 #include "sbz_setup.hpp"
 #include <cstring>

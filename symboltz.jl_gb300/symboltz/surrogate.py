@@ -41,6 +41,13 @@ def sample_box(n, seed=0, sobol=False):
     return BOX[:, 0] + u * (BOX[:, 1] - BOX[:, 0])
 
 
+def needs_solver(errs, tol):
+    """Fallback mask: a cosmology keeps the surrogate's result only if its error estimate is a
+    number at or below tol; NaN or infinite estimates (a network that produced non-finite sources)
+    go to the solver like any estimate above tol."""
+    return ~(np.asarray(errs, dtype=np.float64) <= tol)
+
+
 class MLP:
     """The device MLP (nin → nhidden × width SiLU → nout) of ``sbz_surrogate_*``."""
 
@@ -329,7 +336,7 @@ class SourceSurrogate:
             kprobe = self.probe_kgrid() if kprobe is None else np.asarray(kprobe)
             Fp, taus, vis, prob = self.solve_factors(thetas, ks=kprobe)
             errs = np.array([self.probe_error(t, taus[c], vis[c], Fp[c], kprobe, prob, c, jl, ls_out) for c, t in enumerate(thetas)])
-            fb = errs > tol
+            fb = needs_solver(errs, tol)
         else:  # surrogate only: backgrounds, network, line of sight; no mode is solved
             taus, vis, prob = self.backgrounds(thetas)
             errs = np.full(len(thetas), np.nan)

@@ -4,7 +4,7 @@ The fixtures are the reference's own known answers for this path:
   * class_Pk.txt   <- test/class_Pk.dat  (k [H0/c], P(k) [(c/H0)^3]; CLASS, ΛCDM(lmax=5)+Planck18)
   * class_Cl.txt   <- test/class_Cl.dat  (l, D_l^TT, D_l^EE, D_l^φφ; same model)
   * quadrature.txt <- paper/aa57450-25.tex:1370-1395 (momentum bins x_i and weights W_i, N=1..8)
-Usage: python tests/golden/make_golden.py [reference_root]
+Usage: python tests/golden/make_golden.py REFERENCE_ROOT   (the SymBoltz.jl checkout)
 """
 import os
 import re
@@ -36,4 +36,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py REFERENCE_ROOT")
+    main(sys.argv[1])

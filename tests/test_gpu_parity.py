@@ -64,35 +64,32 @@ def test_pk_matches_oracle(S, prob5, bg5, golden):
 
 @pytest.mark.parametrize("tol,bar", [(1e-5, 1e-3), (1e-7, 2e-5)])
 def test_sources_match_oracle(S, prob5, tol, bar):
-    """Line-of-sight sources against the oracle at the same integrator tolerance.
+    """Line-of-sight sources against the oracle at the same integrator tolerance, in both precisions.
 
-    FP64 mode uses the oracle's arithmetic for the solution and the step-size control, so the two
-    step sequences stay together and the sources agree to well inside the tolerance (bar).  Mixed
-    mode steers the step size in FP32 (the controller is a heuristic), so its step sequence drifts
-    from the oracle's over thousands of steps and the two become independent integrations at the
-    same tolerance.  There the requirement is accuracy parity: the distance to a converged oracle
-    solution (tolerance / 100) is at most a few times the oracle's own distance, plus a floor of a
-    tenth of the bar.  The pointwise maximum over (k, τ) of an FP32-steered integration moves with
-    any last-bit change of its inputs (three such changes gave 2.9, 3.7 and 4.3 times the oracle's
-    distance at rtol 1e-5), so the factor is 5; C_l and P(k) parity are tested at 1e-4 elsewhere."""
+    The error norm and the step-size controller are FP64 in both precisions, like the oracle's, and
+    the stage solutions are FP64 after refinement, so the step sequences stay together and the
+    sources agree to well inside the tolerance (bar, relative to each mode's largest source value).
+    Also, measured against a converged oracle solution (tolerance / 100), the GPU solution is no
+    further off than three times the oracle's own distance plus a tenth of the bar."""
     M = S.ΛCDM(lmax=5)
     fp64 = prob5.opts.precision == 0
     prob = S.CosmologyProblem(M, S.parameters_Planck18(M), pt_rtol=tol, pt_atol=tol,
                               precision="fp64" if fp64 else "mixed")
     bgo = O.Background(O.PLANCK18, MODEL5, pt_rtol=tol, pt_atol=tol)
     ks = np.array([2.0, 50.0, 300.0, 2000.0])
-    taus = np.linspace(bgo.tau0 * 0.01, bgo.tau0 * 0.999, 64)
+    # S_E and S_ψ carry 1/χ² and 1/χ (χ = τ0 - τ): near τ0 they magnify the 1e-8 relative difference
+    # of the two background integrations' τ0 by τ0/χ, so the grid stops at χ = 0.01 τ0
+    taus = np.linspace(bgo.tau0 * 0.01, bgo.tau0 * 0.99, 64)
     out, st, _ = S.solvept(prob, ks, 1e-6, saveat=taus, output="sources")
     ref, sto, _ = bgo.solve_pt(ks, 1e-6, taus, mode=0)
     conv, stc, _ = O.Background(O.PLANCK18, MODEL5, pt_rtol=tol / 100, pt_atol=tol / 100).solve_pt(ks, 1e-6, taus, mode=0)
     assert np.all(st == 0) and np.all(sto == 0) and np.all(stc == 0)
     for s in range(3):
         scale = np.max(np.abs(conv[:, :, s]), axis=1, keepdims=True) + 1e-300
-        if fp64:
-            assert np.max(np.abs(out[:, :, s] - ref[:, :, s]) / scale) < bar, s
+        assert np.max(np.abs(out[:, :, s] - ref[:, :, s]) / scale) < bar, s
         ours = np.max(np.abs(out[:, :, s] - conv[:, :, s]) / scale)
         theirs = np.max(np.abs(ref[:, :, s] - conv[:, :, s]) / scale)
-        assert ours <= (3 if fp64 else 5) * theirs + 0.1 * bar, (s, ours, theirs)
+        assert ours <= 3 * theirs + 0.1 * bar, (s, ours, theirs)
 
 
 def test_state_matches_oracle(S, prob5):
@@ -188,8 +185,11 @@ def test_rhs_matches_oracle(S, prob5, bg5):
             fo, Jo, fto = bg5.rhs(k, tau, Yo[i], jac=True)
             scale = np.abs(Jo) @ np.abs(Yo[i]) + 1e-300
             np.testing.assert_array_less(np.abs(f[i, idx] - fo) / scale, 1e-6, err_msg=f"f tau={tau} k={k}")
+            # ∂f/∂τ from the derivatives of the tabulated coefficients (the table's Hermite slopes)
+            # against the oracle's exact derivatives through the background spline: measured at most
+            # 3.1e-7 of the largest entry (at recombination, where κ̇ changes fastest)
             tscale = np.abs(fto).max() + 1e-300
-            assert np.max(np.abs(ft[i, idx] - fto)) / tscale < 1e-3, (tau, k)
+            assert np.max(np.abs(ft[i, idx] - fto)) / tscale < 1e-6, (tau, k)
 
 
 def test_batched_cosmologies_match_single_solves(S):

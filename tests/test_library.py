@@ -185,3 +185,11 @@ def test_adaptive_refinement_matches_the_reference_rule():
     np.testing.assert_allclose(vals[:, 0, :], fun(got)[:, 0, :])
     with pytest.raises(ValueError):
         S.refine_grid(fun, ks0, atol=1e-12, ktransform=(f, finv), maxks=64)
+
+
+def test_surrogate_routing_sends_non_finite_estimates_to_the_solver():
+    """A cosmology keeps the surrogate's C_l only when its error estimate is a number within the
+    tolerance: NaN and infinite estimates fall back to the solver like estimates above it."""
+    from symboltz.surrogate import needs_solver
+    errs = np.array([1e-4, 1e-3, 2e-3, np.nan, np.inf, 0.0])
+    np.testing.assert_array_equal(needs_solver(errs, 1e-3), [False, False, True, True, True, False])

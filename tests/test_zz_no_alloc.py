@@ -76,3 +76,31 @@ def test_noalloc_rejects_sizes_beyond_the_scratch():
     assert 2 * ((len(ks) + 1 + 31) // 32 * 32) + (len(ks) + 1) * 1040 <= cap
     got = _noalloc(L, torch, ks, P0, ThA, ThB)
     np.testing.assert_allclose(got, _reference(L, ks, P0, ThA, ThB), rtol=RTOL, atol=1e-12 * np.max(np.abs(got)))
+
+
+def test_noalloc_warm_calls_take_no_device_memory():
+    """The entry's promise itself: once loaded, repeated calls leave the device's free memory
+    unchanged (a cudaMalloc inside it, even one freed again before returning, would show up as a
+    changed reading or as a synchronising allocation the caller's pool cannot see)."""
+    torch = pytest.importorskip("torch")
+    from symboltz import _lib
+    L = _lib.lib()
+    ks, P0, ThA, ThB = _case(5, 900, 64)
+    dev = [torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda") for a in (ks, P0, ThA, ThB)]
+    out = torch.zeros(64, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    args = (len(ks), *[C.c_void_p(t.data_ptr()) for t in dev[:2]], 64, *[C.c_void_p(t.data_ptr()) for t in dev[2:]],
+            C.c_void_p(out.data_ptr()), C.c_void_p(stream.cuda_stream))
+    assert L.sbz_cl_integrate_noalloc(*args) == 0, L.sbz_last_error()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    reserved0 = torch.cuda.memory_reserved()
+    for _ in range(20):
+        assert L.sbz_cl_integrate_noalloc(*args) == 0, L.sbz_last_error()
+        free_mid, _ = torch.cuda.mem_get_info()
+        assert free_mid == free0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.memory_reserved() == reserved0
+    np.testing.assert_allclose(out.cpu().numpy(), _reference(L, ks, P0, ThA, ThB), rtol=RTOL,
+                               atol=1e-12 * float(torch.max(torch.abs(out))))
