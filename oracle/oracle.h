@@ -87,6 +87,8 @@ void orc_cl_integrate(int nk, const double* ks, const double* P0, int nl, const 
                       const double* ThB, double* Cl);
 /* Natural cubic spline through (x,y) evaluated at xq (DataInterpolations CubicSpline). */
 void orc_cubic_spline(int n, const double* x, const double* y, int nq, const double* xq, double* out);
+/* m such splines at once, columns of Y[i * m + c] -> out[q * m + c] (OpenMP over columns). */
+void orc_cubic_spline_columns(int n, const double* x, int m, const double* Y, int nq, const double* xq, double* out);
 
 #ifdef __cplusplus
 }

@@ -85,6 +85,7 @@ def lib():
         L.orc_los_integrate.argtypes = [C.c_void_p, C.c_int, dp, C.c_int, dp, C.c_int, dp, C.c_int, dp]
         L.orc_cl_integrate.argtypes = [C.c_int, dp, dp, C.c_int, dp, dp, dp]
         L.orc_cubic_spline.argtypes = [C.c_int, dp, dp, C.c_int, dp, dp]
+        L.orc_cubic_spline_columns.argtypes = [C.c_int, dp, C.c_int, dp, C.c_int, dp, dp]
         _lib = L
     return _lib
 
@@ -293,6 +294,16 @@ def cl_integrate(ks, P0, ThA, ThB):
     return Cl
 
 
+def cubic_spline_columns(x, Y, xq):
+    """Natural cubic splines through (x, Y[:, c]) for every column c, evaluated at xq -> [len(xq), m]."""
+    x, xp = _d(x); xq, qp = _d(xq)
+    Y = np.ascontiguousarray(Y, dtype=np.float64).reshape(len(x), -1)
+    out = np.zeros((len(xq), Y.shape[1]))
+    lib().orc_cubic_spline_columns(len(x), xp, Y.shape[1], Y.ctypes.data_as(C.POINTER(C.c_double)), len(xq), qp,
+                                   out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
 def cubic_spline(x, y, xq):
     x, xp = _d(x); y, yp = _d(y); xq, qp = _d(xq)
     out = np.zeros(len(xq))
@@ -360,3 +371,35 @@ def spectrum_cmb(bg: Background, modes, jl: BesselCache, ls_out=None, *, kinterp
     if return_parts:
         return out, dict(status=status, stats=stats, taus=taus, ks_fine=ks_fine, Sc=Sc, Th=Th)
     return out
+
+
+def spectrum_cmb_kspline(bg: Background, ks, taus, jl: BesselCache, ls_out, modes=("TT", "TE", "EE"), dkt0=np.pi,
+                         return_parts=False, sources=None):
+    """spectrum_cmb (src/observables/angular.jl:260-341) with the sources solved at ks and interpolated
+    to the fine grid lingrid(ks[0], ks[-1], step=Δkτ0/τ0) by natural cubic splines in log k, on the
+    given τ grid (the last time's sources set to zero), T and E only; D_l at ls_out (l-spline).
+    sources: coarse sources [k][tau][3] to use instead of solving."""
+    ks = np.asarray(ks, dtype=np.float64)
+    taus = np.asarray(taus, dtype=np.float64)
+    if sources is None:
+        Sc, status, stats = bg.solve_pt(ks, bg.t[0], taus, mode=0)  # [k][tau][3]
+    else:
+        Sc, status, stats = np.asarray(sources, dtype=np.float64), np.zeros(len(ks), dtype=np.int32), None
+    kf = lingrid(ks[0], ks[-1], step=dkt0 / bg.tau0)
+    Sf = cubic_spline_columns(np.log(ks), Sc[:, :, :2].reshape(len(ks), -1), np.log(kf)).reshape(len(kf), len(taus), 2)
+    Sf = np.ascontiguousarray(Sf.transpose(1, 0, 2))
+    Sf[-1] = 0.0
+    Th = los_integrate(Sf, taus, kf, jl)
+    ls = jl.l.astype(np.float64)
+    Th[:, :, 0] /= kf[:, None]
+    Th[:, :, 1] *= np.sqrt((ls + 2) * (ls + 1) * ls * (ls - 1))[None, :] / kf[:, None] ** 2
+    P0 = bg.primordial(kf)
+    pos = {"T": 0, "E": 1}
+    out = []
+    for mode in modes:
+        Cl = cl_integrate(kf, P0, Th[:, :, pos[mode[0]]], Th[:, :, pos[mode[-1]]]) * ls * (ls + 1) / (2 * np.pi)
+        out.append(cubic_spline(ls, Cl, np.asarray(ls_out, dtype=np.float64)))
+    Dl = np.stack(out, axis=1)
+    if return_parts:
+        return Dl, dict(status=status, stats=stats, nk_fine=len(kf))
+    return Dl

@@ -21,6 +21,7 @@
 #include "oracle.h"
 #include "jet.hpp"
 #include <vector>
+#include <cstdint>
 #include <algorithm>
 #include <cstring>
 #include <cstdio>
@@ -982,14 +983,16 @@ template <class S> struct SparseAcc {
 struct SparsePtSys : PtSys {
   const SparsePattern& SP;
   std::vector<double> vals, A, dinv;
-  std::vector<Jet<1>> jvals;
-  std::vector<int> piv, touched, lptr, lidx, uptr, uidx;
+  std::vector<Jet<1>> jvals, sv;
+  std::vector<int> piv, lptr, lidx, uptr, uidx, rows, ucols;
   std::vector<double> lval, uval, work;
-  std::vector<char> mark;
+  int nwords;
+  std::vector<uint64_t> rowbits, colbits;
   SparsePtSys(const orc_bg& B_, double k_, const SparsePattern& sp) : PtSys(B_, k_), SP(sp) {
     const size_t nnz = SP.row.size();
-    vals.resize(nnz); jvals.resize(nnz); A.assign((size_t)n * n, 0.0); dinv.resize(n); piv.resize(n); work.resize(n);
-    mark.assign((size_t)n * n, 0);
+    vals.resize(nnz); jvals.resize(nnz); sv.resize(nnz); A.assign((size_t)n * n, 0.0); dinv.resize(n); piv.resize(n); work.resize(n);
+    nwords = (n + 63) / 64;
+    rowbits.assign((size_t)n * nwords, 0); colbits.assign((size_t)n * nwords, 0);
   }
   void rhs(double t, const double* y, double* f) override {
     PtCoef<double> C; pt_coef_spline<double>(B, t, C);
@@ -1006,51 +1009,85 @@ struct SparsePtSys : PtSys {
     pt_assemble<Jet<1>>(P, L, k, C, acc, pPsij.data(), pPhidj.data());
     for (int i = 0; i < n; ++i) ft[i] = 0;
     for (size_t e = 0; e < jvals.size(); ++e) ft[SP.row[e]] += jvals[e].c[1] * y[SP.col[e]];
-    // W in elimination order; clear what the previous factorisation left (pattern + fill)
-    for (int p : touched) { A[p] = 0.0; mark[p] = 0; }
-    touched.clear();
-    for (size_t e = 0; e < jvals.size(); ++e) {
-      const int p = SP.iperm[SP.row[e]] * n + SP.iperm[SP.col[e]];
-      A[p] -= jvals[e].c[0];
-      if (!mark[p]) { mark[p] = 1; touched.push_back(p); }
+    // W in elimination order.  Row and column bitmaps track the nonzeros (pattern + fill), so the
+    // elimination touches nonzeros only; clear what the previous factorisation left.
+    const int nw = nwords;
+    for (int i = 0; i < n; ++i) {
+      uint64_t* rb = &rowbits[(size_t)i * nw];
+      for (int w = 0; w < nw; ++w) {
+        for (uint64_t b = rb[w]; b; b &= b - 1) A[(size_t)i * n + 64 * w + __builtin_ctzll(b)] = 0.0;
+        rb[w] = 0;
+      }
     }
-    for (int i = 0; i < n; ++i) { const int p = i * n + i; A[p] += ihg; if (!mark[p]) { mark[p] = 1; touched.push_back(p); } }
+    std::fill(colbits.begin(), colbits.end(), 0);
+    auto setbit = [&](int i, int j) {
+      rowbits[(size_t)i * nw + (j >> 6)] |= 1ull << (j & 63);
+      colbits[(size_t)j * nw + (i >> 6)] |= 1ull << (i & 63);
+    };
+    for (size_t e = 0; e < jvals.size(); ++e) {
+      const int r = SP.iperm[SP.row[e]], c = SP.iperm[SP.col[e]];
+      A[(size_t)r * n + c] -= jvals[e].c[0];
+      setbit(r, c);
+    }
+    for (int i = 0; i < n; ++i) { A[(size_t)i * n + i] += ihg; setbit(i, i); }
     lptr.assign(1, 0); uptr.assign(1, 0); lidx.clear(); lval.clear(); uidx.clear(); uval.clear();
-    std::vector<int> rows, ucols;
     for (int kk = 0; kk < n; ++kk) {
-      // nonzero rows of column kk at or below the diagonal
+      // candidate pivots: nonzero rows of column kk at or below the diagonal
       rows.clear();
       double mx = 0; int pbest = -1;
-      for (int i = kk; i < n; ++i) {
-        const double a = A[i * n + kk];
-        if (a != 0) { rows.push_back(i); if (std::fabs(a) > mx) { mx = std::fabs(a); pbest = i; } }
+      const uint64_t* cb = &colbits[(size_t)kk * nw];
+      for (int w = kk >> 6; w < nw; ++w) {
+        uint64_t b = cb[w];
+        if (w == (kk >> 6)) b &= ~0ull << (kk & 63);
+        for (; b; b &= b - 1) {
+          const int i = 64 * w + __builtin_ctzll(b);
+          const double a = std::fabs(A[(size_t)i * n + kk]);
+          rows.push_back(i);
+          if (a > mx) { mx = a; pbest = i; }
+        }
       }
       if (!(mx > 0) || !std::isfinite(mx)) return false;
       int p = kk;
-      if (!(std::fabs(A[kk * n + kk]) >= 0.1 * mx)) p = pbest;
+      if (!(std::fabs(A[(size_t)kk * n + kk]) >= 0.1 * mx)) p = pbest;
       piv[kk] = p;
-      if (p != kk) {
-        for (int j = 0; j < n; ++j) {
-          std::swap(A[kk * n + j], A[p * n + j]);
-          for (int q : {kk * n + j, p * n + j}) if (!mark[q]) { mark[q] = 1; touched.push_back(q); }
+      if (p != kk) {  // swap rows kk and p over their nonzero columns, and the bitmaps with them
+        uint64_t* ra = &rowbits[(size_t)kk * nw];
+        uint64_t* rp = &rowbits[(size_t)p * nw];
+        for (int w = 0; w < nw; ++w) {
+          for (uint64_t b = ra[w] | rp[w]; b; b &= b - 1) {
+            const int j = 64 * w + __builtin_ctzll(b);
+            std::swap(A[(size_t)kk * n + j], A[(size_t)p * n + j]);
+            uint64_t* c = &colbits[(size_t)j * nw];
+            const bool bk = (c[kk >> 6] >> (kk & 63)) & 1, bp = (c[p >> 6] >> (p & 63)) & 1;
+            if (bk != bp) { c[kk >> 6] ^= 1ull << (kk & 63); c[p >> 6] ^= 1ull << (p & 63); }
+          }
+          std::swap(ra[w], rp[w]);
         }
         for (int& r : rows) if (r == p) r = kk; else if (r == kk) r = p;
       }
-      const double d = 1.0 / A[kk * n + kk];
+      const double d = 1.0 / A[(size_t)kk * n + kk];
       dinv[kk] = d;
       ucols.clear();
-      for (int j = kk + 1; j < n; ++j) if (A[kk * n + j] != 0) { ucols.push_back(j); uidx.push_back(j); uval.push_back(A[kk * n + j]); }
+      const uint64_t* rk = &rowbits[(size_t)kk * nw];
+      for (int w = kk >> 6; w < nw; ++w) {
+        uint64_t b = rk[w];
+        if (w == (kk >> 6)) b &= (kk & 63) == 63 ? 0 : ~0ull << ((kk & 63) + 1);
+        for (; b; b &= b - 1) {
+          const int j = 64 * w + __builtin_ctzll(b);
+          ucols.push_back(j); uidx.push_back(j); uval.push_back(A[(size_t)kk * n + j]);
+        }
+      }
       uptr.push_back((int)uidx.size());
+      const double* Rk = &A[(size_t)kk * n];
       for (int i : rows) {
         if (i == kk) continue;
-        const double l = A[i * n + kk] * d;
+        const double l = A[(size_t)i * n + kk] * d;
         lidx.push_back(i); lval.push_back(l);
-        double* Ri = &A[i * n];
-        const double* Rk = &A[kk * n];
+        double* Ri = &A[(size_t)i * n];
+        uint64_t* ri = &rowbits[(size_t)i * nw];
         for (int j : ucols) {
-          const int q = i * n + j;
           Ri[j] -= l * Rk[j];
-          if (!mark[q]) { mark[q] = 1; touched.push_back(q); }
+          if (!((ri[j >> 6] >> (j & 63)) & 1)) setbit(i, j);
         }
       }
       lptr.push_back((int)lidx.size());
@@ -1058,7 +1095,7 @@ struct SparsePtSys : PtSys {
     return true;
   }
   void source_products(const PtCoef<Jet<1>>& C, const double* y, double* f, double* g) override {
-    std::vector<Jet<1>> sv(jvals.size(), Jet<1>(0.0));
+    std::fill(sv.begin(), sv.end(), Jet<1>(0.0));
     SparseAcc<Jet<1>> acc{SP, sv.data()};
     pt_assemble<Jet<1>>(P, L, k, C, acc, pPsij.data(), pPhidj.data());
     for (int i = 0; i < n; ++i) { f[i] = 0; g[i] = 0; }

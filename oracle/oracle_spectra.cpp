@@ -219,3 +219,28 @@ extern "C" void orc_cubic_spline(int n, const double* x, const double* y, int nq
     out[q] = z[i] * A * A * A / (6 * h) + z[i + 1] * B * B * B / (6 * h) + (y[i + 1] / h - z[i + 1] * h / 6) * B + (y[i] / h - z[i] * h / 6) * A;
   }
 }
+
+// m natural cubic splines through (x, Y[:, c]) evaluated at xq, columns in parallel:
+// Y[i * m + c] -> out[q * m + c] (the k-interpolation of the sources, one spline per (τ, source)).
+extern "C" void orc_cubic_spline_columns(int n, const double* x, int m, const double* Y, int nq, const double* xq, double* out) {
+  std::vector<int> iv(nq);
+  for (int q = 0; q < nq; ++q) {
+    int i = (int)(std::upper_bound(x, x + n, xq[q]) - x) - 1;
+    iv[q] = std::max(0, std::min(i, n - 2));
+  }
+#pragma omp parallel
+  {
+    std::vector<double> y(n), z(n);
+#pragma omp for schedule(static)
+    for (int c = 0; c < m; ++c) {
+      for (int i = 0; i < n; ++i) y[i] = Y[(size_t)i * m + c];
+      Spline::second(n, x, y.data(), z.data());
+      for (int q = 0; q < nq; ++q) {
+        const int i = iv[q];
+        const double t = xq[q], h = x[i + 1] - x[i], A = x[i + 1] - t, B = t - x[i];
+        out[(size_t)q * m + c] = z[i] * A * A * A / (6 * h) + z[i + 1] * B * B * B / (6 * h) + (y[i + 1] / h - z[i + 1] * h / 6) * B +
+                                 (y[i] / h - z[i] * h / 6) * A;
+      }
+    }
+  }
+}

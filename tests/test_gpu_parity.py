@@ -49,17 +49,32 @@ def test_background_matches_oracle(S, prob5, bg5):
     assert abs(bg.taurec[0] / bg5.taurec - 1) < 1e-5
 
 
-def test_pk_matches_oracle(S, prob5, bg5, golden):
+def test_pk_matches_oracle(S, prob5, golden):
+    """P(k) against the oracle at matched integrator tolerances, and against the reference's CLASS
+    fixture at the reference's own settings.
+
+    Parity is measured at rtol = atol = 1e-7, where the integration error of P(k) (the oracle's own
+    distance to a converged solution, at most 1.0e-4 over these k) is below the bar.  At the
+    reference's default 1e-5 that error is up to 2e-3 (at the lowest k) and two integrations whose
+    coefficient evaluations differ in the last bits (the device table against the oracle's spline)
+    can take a different accept/reject decision and end up that far apart."""
     d = np.loadtxt(os.path.join(golden, "class_Pk.txt"))
     ks = d[:, 0]
-    P, st = S.spectrum_matter(prob5, ks, return_status=True)
-    Po, sto, _ = O.spectrum_matter(bg5, ks)
+    M = S.ΛCDM(lmax=5)
+    prec = "fp64" if prob5.opts.precision == 0 else "mixed"
+    tight = S.CosmologyProblem(M, S.parameters_Planck18(M), precision=prec, pt_rtol=1e-7, pt_atol=1e-7)
+    P, st = S.spectrum_matter(tight, ks, return_status=True)
+    bgo = O.Background(O.PLANCK18, MODEL5, pt_rtol=1e-7, pt_atol=1e-7)
+    Po, sto, _ = O.spectrum_matter(bgo, ks)
     assert np.all(st == 0) and np.all(sto == 0)
     rel = np.abs(P / Po - 1)
     assert np.max(rel[ks > 0.15]) < 1e-4, np.max(rel)
-    assert np.linalg.norm(P - Po) <= 1e-4 * np.linalg.norm(Po)
-    # and against the reference's CLASS fixture at its own tolerance (test/runtests.jl:871-876)
-    assert np.linalg.norm(P - d[:, 1]) <= 1e-3 * np.linalg.norm(d[:, 1])
+    assert np.linalg.norm(P - Po) <= 1e-5 * np.linalg.norm(Po)
+    # the reference's settings (rtol = atol = 1e-5) against its CLASS fixture (test/runtests.jl:871-876)
+    P5, st5 = S.spectrum_matter(prob5, ks, return_status=True)
+    assert np.all(st5 == 0)
+    assert np.linalg.norm(P5 - d[:, 1]) <= 1e-3 * np.linalg.norm(d[:, 1])
+    assert np.linalg.norm(P5 - P) <= 1e-4 * np.linalg.norm(P)
 
 
 @pytest.mark.parametrize("tol,bar", [(1e-5, 1e-3), (1e-7, 2e-5)])
@@ -151,6 +166,9 @@ def test_los_and_cl_match_oracle(S):
 
 
 def test_cmb_matches_oracle_and_class(S, golden, bg5):
+    """D_l TT/EE/ψψ against the oracle at matched tolerances (rtol 1e-6, atol 3e-8, where the
+    integration error of the low-l D_l is far below the bar; see test_pk_matches_oracle), and the
+    reference's default settings against its CLASS fixture at the reference's tolerance."""
     d = np.loadtxt(os.path.join(golden, "class_Cl.txt"))
     lc = d[:, 0]
     ls = np.unique(np.round(np.exp(np.linspace(np.log(lc[0]), np.log(lc[-1]), 200))).astype(int))
@@ -162,8 +180,10 @@ def test_cmb_matches_oracle_and_class(S, golden, bg5):
     # integrations place knots slightly differently, so parity is measured on one shared grid
     t = bg5.t[bg5.t >= 1e-2]
     taus = t[0] + (bg5.tau0 * (1 - 1e-12) - t[0]) * S.cosgrid(0.0, 1.0, length=300)
-    Dg = S.spectrum_cmb(["TT", "EE", "ψψ"], prob, jl, lc, normalization="Dl", taus=taus)
-    Do = O.spectrum_cmb(bg5, ["TT", "EE", "ψψ"], O.BesselCache(ls), lc, taus=taus)
+    tight = S.CosmologyProblem(M, S.parameters_Planck18(M), pt_rtol=1e-6, pt_atol=3e-8)
+    Dg = S.spectrum_cmb(["TT", "EE", "ψψ"], tight, jl, lc, normalization="Dl", taus=taus)
+    bgt = O.Background(O.PLANCK18, MODEL5, pt_rtol=1e-6, pt_atol=3e-8)
+    Do = O.spectrum_cmb(bgt, ["TT", "EE", "ψψ"], O.BesselCache(ls), lc, taus=taus)
     for j in range(3):
         assert np.linalg.norm(Dg[:, j] - Do[:, j]) <= 1e-4 * np.linalg.norm(Do[:, j]), j
         assert np.linalg.norm(Dl[:, j] - d[:, j + 1]) <= 2e-3 * np.linalg.norm(d[:, j + 1]), j
@@ -346,3 +366,30 @@ def test_device_table_matches_oracle(S, bg5):
     ek = np.exp(-b[:, 3])  # e^{-κ} from the oracle's κ, where the sources see it (early on κ is huge)
     seen = ek > 1e-3
     np.testing.assert_allclose(c[seen, 4], ek[seen], rtol=1e-5)
+
+
+def test_spline_kinterp_pipeline_matches_oracle(S):
+    """The device pipeline with natural-spline k-interpolation (the bench's interpolator: splines in
+    log k through the coarse modes, sbz_spectrum_cmb_sources) against the oracle's restatement on the
+    same smooth synthetic sources: both are linear in the sources, so they agree to rounding."""
+    rng = np.random.default_rng(3)
+    M = S.ΛCDM(lmax=5)
+    prob = S.CosmologyProblem(M, S.parameters_Planck18(M))
+    bg = prob.solvebg()
+    ks = S.k_from_hMpc(S.loggrid(1e-4, 0.5, length=57))
+    t = bg.t(0)
+    t = t[t >= 1e-2]
+    taus = t[0] + (bg.tau0[0] - t[0]) * S.cosgrid(0.0, 1.0, length=180)
+    lk, lt = np.log(ks)[:, None], (taus / taus[-1])[None, :]
+    src = np.zeros((len(ks), len(taus), 3))
+    for s in range(3):
+        a = rng.uniform(0.5, 2.0, 3)
+        src[:, :, s] = np.sin(a[0] * lk + 3 * a[1] * lt) * np.exp(-((lt - 0.02 * a[2]) ** 2) / 0.01) + 0.1 * np.cos(a[2] * lk)
+    ls = np.unique(np.round(np.exp(np.linspace(np.log(2), np.log(400), 40))).astype(int))
+    lall = np.arange(2, 401)
+    Dg = S.spectrum_cmb(["TT", "TE", "EE"], prob, S.SphericalBesselCache(ls), lall, kinterp=S.CubicSplineInterpolator(ks, f=np.log),
+                        taus=taus, normalization="Dl", sources=src)
+    bgo = O.Background(O.PLANCK18, MODEL5)
+    bgo.tau0 = float(bg.tau0[0])  # the device pipeline's fine k grid uses the device background's τ0
+    Do = O.spectrum_cmb_kspline(bgo, ks, taus, O.BesselCache(ls), lall, sources=src)
+    np.testing.assert_allclose(Dg, Do, rtol=1e-9, atol=1e-12 * np.max(np.abs(Do)))

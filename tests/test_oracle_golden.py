@@ -163,3 +163,23 @@ def test_mlp_oracle_gradient_matches_finite_differences():
                    for e in np.eye(n)])
     np.testing.assert_allclose(g, fd, rtol=1e-6, atol=1e-9)
     assert MO.bf16_round(np.array([1.0, 1.00390625, 3.14159]))[2] == 3.140625
+
+
+def test_sparse_lu_path_equals_dense_checker():
+    """The oracle's sparse-LU path (the timed CPU baseline and the fast checker of the large
+    workloads) integrates the same equations with the same Rodas5P steps as the dense-LU checker:
+    same step counts, sources equal to rounding (the two eliminations order their operations
+    differently), on the massive-ν, l_γ = 30 model at low and intermediate k."""
+    m = dict(lmax_g=30, lmax_nu=10, lmax_h=10, nx=5, Hswitch=1, Heswitch=6, reionization=1)
+    p = dict(O.PLANCK18, m_nu_eV=0.06, N_nu=1.0, Neff=2.0328)
+    ks = np.array([0.05, 3.0, 60.0, 300.0])
+    out = {}
+    for ls in ("dense", "sparse"):
+        bg = O.Background(p, m, linsolve=ls)
+        taus = np.linspace(bg.tau0 * 0.01, bg.tau0 * 0.99, 40)
+        S, st, stats = bg.solve_pt(ks, bg.t[0], taus, mode=0)
+        assert np.all(st == 0)
+        out[ls] = (S, stats)
+    np.testing.assert_array_equal(out["dense"][1], out["sparse"][1])
+    scale = np.max(np.abs(out["dense"][0]), axis=1, keepdims=True) + 1e-300
+    assert np.max(np.abs(out["dense"][0] - out["sparse"][0]) / scale) < 1e-8  # measured 1.5e-9
