@@ -231,6 +231,14 @@ int sbz_surrogate_infer(sbz_surrogate* s, long long n, const float* X, float* Y)
 /* Flat binary weight file: "SBZMLP01", int32 nin, width, nhidden, nout, FP32 parameters. */
 int sbz_surrogate_save(const sbz_surrogate* s, const char* path);
 int sbz_surrogate_load(const char* path, int batch, sbz_surrogate** out);
+/* Flat binary training-set file: "SBZTRN01", int32 nin, int32 nout, int64 nrows, then nrows rows of
+ * nin + nout float32 (inputs, then targets).  The data side of the surrogate's I/O; the reference
+ * has no surrogate, its batched parameter path (parameter_updater, src/solve.jl:271-306) is what
+ * produces the data.  _append creates the file or adds rows to it (the shapes must match);
+ * _read copies rows [first, first + n). */
+int sbz_trainset_append(const char* path, int nin, int nout, long long n, const float* X, const float* Y);
+int sbz_trainset_info(const char* path, int* nin, int* nout, long long* nrows);
+int sbz_trainset_read(const char* path, long long first, long long n, float* X, float* Y);
 
 /* spectrum_cmb(ΘlAs, ΘlBs, P0s, ls, ks) (src/observables/angular.jl:198-223): natural cubic
  * spline through (0,0) and (k, 2/π k² P0 Θ_A Θ_B), integrated exactly.  Th[ik*nl + il]. */

@@ -16,7 +16,7 @@ LIB = os.path.join(LIBDIR, "libsymboltz_gb300.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SRCS = ["sbz_pt.cu", "sbz_pt_f32_w1.cu", "sbz_pt_f32_w24.cu", "sbz_pt_f64_w1.cu", "sbz_pt_f64_w24.cu", "sbz_los.cu", "sbz_capi.cu", "sbz_noalloc.cu", "sbz_mlp.cu", "sbz_surrogate.cu", "sbz_table.cu"]
-CXX_SRCS = ["sbz_background.cpp", "sbz_setup.cpp"]
+CXX_SRCS = ["sbz_background.cpp", "sbz_setup.cpp", "sbz_trainset.cpp"]
 
 
 def _compile(src):

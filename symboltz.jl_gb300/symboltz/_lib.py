@@ -22,7 +22,7 @@ EXPORTS = (
     "sbz_spectrum_matter", "sbz_spectrum_primordial", "sbz_bessel_create", "sbz_bessel_destroy", "sbz_bessel_eval",
     "sbz_los_integrate", "sbz_los_integrate_device", "sbz_cl_integrate", "sbz_cl_integrate_noalloc", "sbz_autotune_pt", "sbz_mlp_gemm", "sbz_surrogate_create", "sbz_surrogate_destroy", "sbz_surrogate_nparams",
     "sbz_surrogate_get_params", "sbz_surrogate_set_params", "sbz_surrogate_set_data", "sbz_surrogate_train",
-    "sbz_surrogate_gradients", "sbz_surrogate_infer", "sbz_surrogate_save", "sbz_surrogate_load", "sbz_spectrum_cmb", "sbz_spectrum_cmb_sources", "sbz_problem_set_stream",
+    "sbz_surrogate_gradients", "sbz_surrogate_infer", "sbz_surrogate_save", "sbz_surrogate_load", "sbz_trainset_append", "sbz_trainset_info", "sbz_trainset_read", "sbz_spectrum_cmb", "sbz_spectrum_cmb_sources", "sbz_problem_set_stream",
     "sbz_problem_timings",
 )
 SBZ_KINTERP_SPLINE, SBZ_KINTERP_BARYCENTRIC = 0, 1
@@ -90,6 +90,10 @@ def lib():
     L.sbz_surrogate_infer.argtypes = [vp, C.c_longlong, fp, fp]
     L.sbz_surrogate_save.argtypes = [vp, C.c_char_p]
     L.sbz_surrogate_load.argtypes = [C.c_char_p, C.c_int, C.POINTER(vp)]
+    fp = C.POINTER(C.c_float)
+    L.sbz_trainset_append.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_longlong, fp, fp]
+    L.sbz_trainset_info.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_longlong)]
+    L.sbz_trainset_read.argtypes = [C.c_char_p, C.c_longlong, C.c_longlong, fp, fp]
     L.sbz_mlp_gemm.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, C.c_int, C.c_int, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp]
     L.sbz_solve_pt_device.argtypes = [vp, C.c_int, vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp]
     L.sbz_pt_rhs.argtypes = [vp, C.c_int, ip, dp, dp, dp, dp, dp]

@@ -48,6 +48,37 @@ def needs_solver(errs, tol):
     return ~(np.asarray(errs, dtype=np.float64) <= tol)
 
 
+def write_training_set(path, X, Y):
+    """Append rows (X [n, nin], Y [n, nout], float32) to the flat SBZTRN01 training-set file at path,
+    creating it if needed (sbz_trainset_append)."""
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    Y = np.ascontiguousarray(Y, dtype=np.float32)
+    if X.ndim != 2 or Y.ndim != 2 or len(X) != len(Y):
+        raise ValueError("X and Y must be 2-d with one row per sample")
+    fp = C.POINTER(C.c_float)
+    L.check(L.lib().sbz_trainset_append(str(path).encode(), X.shape[1], Y.shape[1], len(X), X.ctypes.data_as(fp),
+                                        Y.ctypes.data_as(fp)), "write_training_set")
+
+
+def training_set_info(path):
+    """(nin, nout, nrows) of a training-set file."""
+    a, b, n = C.c_int(), C.c_int(), C.c_longlong()
+    L.check(L.lib().sbz_trainset_info(str(path).encode(), C.byref(a), C.byref(b), C.byref(n)), "training_set_info")
+    return a.value, b.value, n.value
+
+
+def read_training_set(path, first=0, n=None):
+    """Rows [first, first + n) of a training-set file as (X, Y) float32 arrays (all rows by default)."""
+    nin, nout, rows = training_set_info(path)
+    n = rows - first if n is None else n
+    X = np.empty((n, nin), dtype=np.float32)
+    Y = np.empty((n, nout), dtype=np.float32)
+    fp = C.POINTER(C.c_float)
+    L.check(L.lib().sbz_trainset_read(str(path).encode(), first, n, X.ctypes.data_as(fp), Y.ctypes.data_as(fp)),
+            "read_training_set")
+    return X, Y
+
+
 class MLP:
     """The device MLP (nin → nhidden × width SiLU → nout) of ``sbz_surrogate_*``."""
 

@@ -193,3 +193,32 @@ def test_surrogate_routing_sends_non_finite_estimates_to_the_solver():
     from symboltz.surrogate import needs_solver
     errs = np.array([1e-4, 1e-3, 2e-3, np.nan, np.inf, 0.0])
     np.testing.assert_array_equal(needs_solver(errs, 1e-3), [False, False, True, True, True, False])
+
+
+def test_training_set_file_round_trip(tmp_path):
+    """Flat SBZTRN01 training-set files: shards appended one after another read back exactly, in
+    any row range; mismatched shapes, ranges past the end and foreign files are refused."""
+    from symboltz import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("library not built")
+    from symboltz import surrogate as SG
+    rng = np.random.default_rng(0)
+    path = tmp_path / "train.sbz"
+    shards = [(rng.standard_normal((n, 8)).astype(np.float32), rng.standard_normal((n, 7)).astype(np.float32)) for n in (5, 70000, 3)]
+    for X, Y in shards:
+        SG.write_training_set(path, X, Y)
+    assert SG.training_set_info(path) == (8, 7, 70008)
+    X, Y = SG.read_training_set(path)
+    np.testing.assert_array_equal(X, np.concatenate([s[0] for s in shards]))
+    np.testing.assert_array_equal(Y, np.concatenate([s[1] for s in shards]))
+    Xp, Yp = SG.read_training_set(path, first=69990, n=18)
+    np.testing.assert_array_equal(Xp, X[69990:])
+    np.testing.assert_array_equal(Yp, Y[69990:])
+    with pytest.raises(_lib.SbzError):
+        SG.write_training_set(path, np.zeros((2, 6), np.float32), np.zeros((2, 7), np.float32))
+    with pytest.raises(_lib.SbzError):
+        SG.read_training_set(path, first=70000, n=9)
+    bad = tmp_path / "other.bin"
+    bad.write_bytes(b"SBZMLP01" + bytes(16))
+    with pytest.raises(_lib.SbzError):
+        SG.training_set_info(bad)
