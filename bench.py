@@ -42,11 +42,6 @@ METRIC = "k-mode solves/s (cosmologies/s) at <=1e-4 rel C_l err"
 # divided by k²): at rtol 1e-6 every l is within 1.1e-4 of a converged solution for atol 1e-7 and
 # within 1.3e-5 for atol 3e-8 (oracle, Rodas5P, against rtol = atol = 1e-9).
 PT_RTOL, PT_ATOL = 1e-6, 3e-8
-# Lazy refinement threshold for the C_l workload: stages 2-6 skip the FP64 refinement when stage 1's
-# first correction is below 1e-4 of the error weights.  The C_l it gives agree with the fully
-# refined solve (the accuracy field below compares every run against all-FP64); pointwise sources
-# would want the library default 1e-5.
-REFINE_SKIP_CL = 1e-4
 
 
 def workload_grids(S, prob):
@@ -148,7 +143,7 @@ def run_ours(args):
     from symboltz import replicas as R
     rank, world = R.init("nccl")  # replicas: each rank runs the whole workload, no data-path collective
     M = S.ΛCDM(lmax_gamma=MODEL["lmax_gamma"], lmax_nu=MODEL["lmax_nu"], lmax_h=MODEL["lmax_h"], nx=MODEL["nx"])
-    prob = S.CosmologyProblem(M, PARAMS, precision=args.precision, refine_skip=REFINE_SKIP_CL, pt_rtol=PT_RTOL, pt_atol=PT_ATOL)
+    prob = S.CosmologyProblem(M, PARAMS, precision=args.precision, pt_rtol=PT_RTOL, pt_atol=PT_ATOL)
     ks, taus, ls = workload_grids(S, prob)
     jl = S.SphericalBesselCache(ls)
     kinterp = S.CubicSplineInterpolator(ks, f=np.log)
@@ -234,7 +229,7 @@ def run_ours(args):
         "config": {"workload": "LCDM+massive-nu, l_gamma=30, 1000 k log 1e-5..5 h/Mpc, 2000 tau, TT/TE/EE to l=2500",
                    "n_state": prob.nstate, "nk": NK, "ntau": NTAU, "nl_sampled": int(len(ls)), "nk_fine": nk_fine,
                    "precision": args.precision, "pt_rtol": prob.opts.pt_rtol, "pt_atol": prob.opts.pt_atol,
-                   "refine_skip": REFINE_SKIP_CL,
+                   "refinement": "stage 1 of each step (library default)",
                    "l2": "flushed (256 MB write) between steps"},
         "cosmologies_per_s": round(world * K / (dev / 1e3), 4),
         "e2e": {"value": round(e2e_v, 2), "unit": "k-modes/s", "cosmologies_per_s": round(world * K / (e2e / 1e3), 4),
@@ -476,8 +471,8 @@ def run_surrogate(args):
 
 
 def profile_case(args):
-    """Small cases for ncu section captures.  pt: 64 of the 1000 modes (even in log k, the slowest
-    included), sources on 200 times.  los: one spectrum_cmb of the full workload (the line-of-sight
+    """Small cases for ncu section captures, at the workload's tolerances.  pt: 64 of the 1000 modes
+    (even in log k, the slowest included), sources on 200 times.  los: one spectrum_cmb of the full workload (the line-of-sight
     kernel runs once on the full fine k grid; ~1.5 GB on the device).  mlp: the surrogate's training
     step (8 -> 4x512 -> 7, batch 65536) on 2 M synthetic samples, one eager step, the graph capture
     and 4 graph replays, plus a timed run of 200 steps printed first."""
@@ -496,7 +491,7 @@ def profile_case(args):
                               "tflops": round(3 * 2 * 65536 * (64 * 512 + 3 * 512 * 512 + 512 * 64) * args.steps / dt / 1e12, 1)}))
         return
     M = S.ΛCDM(lmax_gamma=MODEL["lmax_gamma"], lmax_nu=MODEL["lmax_nu"], lmax_h=MODEL["lmax_h"], nx=MODEL["nx"])
-    prob = S.CosmologyProblem(M, PARAMS, precision=args.precision)
+    prob = S.CosmologyProblem(M, PARAMS, precision=args.precision, pt_rtol=PT_RTOL, pt_atol=PT_ATOL)
     ks, taus, ls = workload_grids(S, prob)
     if args.profile_case == "pt":
         sel = ks[np.linspace(0, len(ks) - 1, 64).round().astype(int)]

@@ -72,13 +72,12 @@ typedef struct sbz_opts {
   int warps_per_mode;       /* warps integrating one mode: 1, 2 or 4; 0 = chosen from the number of modes */
   int blocks_per_sm;        /* resident thread blocks per SM for the perturbation kernel; 0 = chosen */
   int los_precision;        /* line of sight: SBZ_FP64 or SBZ_MIXED (FP32 interpolation); -1 = as precision */
-  double refine_skip;       /* SBZ_MIXED: stages 2-6 of a step are not refined when stage 1's first correction
-                               is below this (error-weight units); 0 = always refine; < 0 (default) = by launch
-                               shape: 1e-5 for four-warp groups (few modes, run time set by the slowest mode,
-                               where skipping shortens each step: 1.3x on a 1000-mode spectrum) and 0 for
-                               narrower groups (throughput-bound batches, where it measured 11 % slower).
-                               At 1e-5 the sources stay at the fully refined accuracy (1e-4 still gives the
-                               same C_l: the line-of-sight integrals average the unrefined solves' rounding) */
+  double refine_skip;       /* SBZ_MIXED: the later stages (2-8) of a step are refined only when stage 1's
+                               first correction is at or above this (error-weight units); stage 1 is always
+                               refined.  0 = refine every stage; < 0 (default) = never refine the later
+                               stages: on the 1000-mode massive-ν spectrum at rtol 1e-6, atol 3e-8 their FP32
+                               solves leave C_l 3.9e-6 from the all-FP64 solver (5.9e-6 with every stage
+                               refined) at 1.99 s against 2.90 s */
 } sbz_opts;
 
 typedef struct sbz_problem sbz_problem;

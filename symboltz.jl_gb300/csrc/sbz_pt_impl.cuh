@@ -64,6 +64,7 @@ struct ModeMem {
   ST cf[2][kMaxChains];              // forward-eliminated first row of each chain, per vector
   int16_t att[NM];                   // head row a chain row's back substitution depends on, or -1
   int hatt[8];                       // chain attached to head row 3 + q, or -1
+  int hfused;                        // every chain attached to the head is in pair 0 (warp 0's)
   ST Z1[NM + 1], Z2[NM + 1];
   ST H[64], Hinv[64];
   ST hmul[kMaxChains], hcorr[kMaxChains];
@@ -449,8 +450,15 @@ __device__ __forceinline__ void solve_M(const Grp<NW>& g, ModeMem<NW, NSL, ST>& 
       v0[0] *= F.is;
       if (NV > 1) v1[0] *= F.is;
     }
-    g.sync();
-    if (g.wq == 0 && lane < 8) {  // 8x8 head with the chains' couplings: explicit inverse
+    // 8x8 head with the chains' couplings: explicit inverse.  When every chain attached to the
+    // head is in pair 0 (the photon T and P tails), warp 0 has just eliminated them itself and
+    // solves the head at once, without waiting for the other warps' chains.
+    if (W.hfused) {
+      if (g.wq == 0) __syncwarp();
+    } else {
+      g.sync();
+    }
+    if (g.wq == 0 && lane < 8) {
       const int ch = W.hatt[lane];
       ST b0 = v0[3 + lane], b1 = NV > 1 ? v1[3 + lane] : ST(0);
       if (ch >= 0) { const ST hm = W.hmul[ch]; b0 -= hm * W.cf[0][ch]; if (NV > 1) b1 -= hm * W.cf[1][ch]; }
@@ -840,6 +848,11 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
     for (int c = 0; c < M.nchain; ++c) if (M.chAttach[c] == 3 + gt) hc = c;
     W.hatt[gt] = hc;
   }
+  if (gt == 0) {
+    bool f = scan;
+    for (int c = 0; c < M.nchain; ++c) if (M.chAttach[c] >= 0 && c > 1) f = false;
+    W.hfused = f ? 1 : 0;
+  }
 
   for (;;) {
     if (gt == 0) W.item = (int)atomicAdd(A.counter, 1u);
@@ -1027,8 +1040,8 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         for (int sl = 0; sl < NSL; ++sl) b[sl] = f0[sl] + h * TB::d(0) * ft[sl];
         float c1 = 1e30f;
         stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, isk, b, U[0], &c1);
-        // lazy refinement: the later stages share stage 1's W; when its first FP64 correction is
-        // already below refine_skip (error-weight units) the FP32 solves are accurate and are not refined
+        // the later stages share stage 1's W; they are refined only when stage 1's first FP64
+        // correction is at or above refine_skip (error-weight units; the default never refines them)
         const int rk = (A.refine > 0 && c1 < A.refine_skip) ? 0 : A.refine;
 #pragma unroll
         for (int st = 1; st < TB::S; ++st) {

@@ -6,11 +6,11 @@ each cosmology's visibility function.  It is trained on factors computed by the 
 solver (output "factors") with the library's own BF16 tensor-core forward/backward kernels
 (``sbz_surrogate_*``), and evaluated the same way.
 Its sources go through the regular k-interpolation → line-of-sight → C_ℓ pipeline
-(``sbz_spectrum_cmb_sources``).  Each cosmology gets an error estimate in the C_ℓ metric: 48 probe
-modes are also solved with the real solver, and D_ℓ from the surrogate's and the solver's sources
-at those modes (same pipeline, same probe grid) are compared; a cosmology whose estimate exceeds
-the tolerance is recomputed with the solver (fallback), which therefore remains the reference for
-every result.
+(``sbz_spectrum_cmb_sources``).  Each cosmology gets an error estimate in the C_ℓ metric, from the
+disagreement of two networks trained from different initialisations (no mode solved), or from 48
+probe modes solved with the real solver; a cosmology whose estimate exceeds the tolerance is
+recomputed by the solver (all flagged cosmologies' modes in one launch), which therefore remains
+the reference for every result.
 """
 import ctypes as C
 
@@ -167,10 +167,18 @@ class SourceSurrogate:
 
     KPOW = np.array([0, 0, 1, 2, 0, 1, 2])  # factors are learned as f_j / k^KPOW[j]
 
-    def __init__(self, M, ks, ntau=500, width=512, nhidden=4, batch=65536, seed=0):
+    @property
+    def net(self):
+        return self.nets[0]
+
+    def __init__(self, M, ks, ntau=500, width=512, nhidden=4, batch=65536, seed=0, members=2, pt_rtol=1e-5, pt_atol=1e-5):
+        """members: networks trained from different initialisations on the same data; the sources are
+        their mean and their disagreement is the per-cosmology error estimate.  pt_rtol, pt_atol: the
+        solver tolerances of the training data and of the fallback."""
         self.M, self.ks, self.ntau = M, np.asarray(ks, dtype=np.float64), ntau
         self.logk = (np.log(self.ks.min()), np.log(self.ks.max()))
-        self.net = MLP(8, width, nhidden, 7, batch, seed)
+        self.nets = [MLP(8, width, nhidden, 7, batch, seed + 7919 * i) for i in range(max(1, members))]
+        self.pt_rtol, self.pt_atol = pt_rtol, pt_atol
         self.mean = np.zeros(7)
         self.scale = np.ones(7)
         self.env_lk = np.array([-1.0, 1.0])  # k envelope: log k feature nodes and log RMS per factor
@@ -217,7 +225,8 @@ class SourceSurrogate:
         with taus [ncos][ntau], visibilities [ncos][4][ntau] and the problem."""
         from . import CosmologyProblem, solvept
         ks = self.ks if ks is None else np.asarray(ks, dtype=np.float64)
-        prob = CosmologyProblem(self.M, [box_params(t) for t in thetas], precision=precision)
+        prob = CosmologyProblem(self.M, [box_params(t) for t in thetas], precision=precision, pt_rtol=self.pt_rtol,
+                                pt_atol=self.pt_atol)
         bg = prob.solvebg()
         if np.any(bg.status != 0):
             raise L.SbzError("background failed for a cosmology of the box")
@@ -234,7 +243,7 @@ class SourceSurrogate:
         """Times [ncos][ntau], visibilities [ncos][4][ntau] and the problem of the given parameter
         points from their backgrounds alone (no perturbation modes solved)."""
         from . import CosmologyProblem
-        prob = CosmologyProblem(self.M, [box_params(t) for t in thetas])
+        prob = CosmologyProblem(self.M, [box_params(t) for t in thetas], pt_rtol=self.pt_rtol, pt_atol=self.pt_atol)
         bg = prob.solvebg()
         if np.any(bg.status != 0):
             raise L.SbzError("background failed for a cosmology of the box")
@@ -302,35 +311,44 @@ class SourceSurrogate:
         Z = Y / self.envelope(X[:, 6])
         self.mean = Z.mean(axis=0)
         self.scale = Z.std(axis=0) + 1e-30
-        self.net.set_data(X, ((Z - self.mean) / self.scale).astype(np.float32))
+        Zn = ((Z - self.mean) / self.scale).astype(np.float32)
         losses = []
-        per = max(1, steps // chunks)
-        done = 0
-        while done < steps:
-            n = min(per, steps - done)
-            rate = lr * (lr_final / lr) ** (done / max(1, steps))
-            losses.append(self.net.train(n, rate))
-            done += n
-        return losses
+        for net in self.nets:
+            net.set_data(X, Zn)
+            per = max(1, steps // chunks)
+            done = 0
+            lm = []
+            while done < steps:
+                n = min(per, steps - done)
+                rate = lr * (lr_final / lr) ** (done / max(1, steps))
+                lm.append(net.train(n, rate))
+                done += n
+            losses.append(lm)
+        return losses[0] if len(losses) == 1 else losses
 
     def mse(self, X, Y):
-        """Mean squared error of the network on (X, Y) in standardised units (all rows)."""
-        P = self.net.infer(X).astype(np.float64)
+        """Mean squared error of the members' mean on (X, Y) in standardised units (all rows)."""
+        P = np.mean([net.infer(X).astype(np.float64) for net in self.nets], axis=0)
         return float(np.mean((P - self.normalise(X, Y)) ** 2))
 
     # ---- prediction ------------------------------------------------------------------------
-    def predict_factors(self, theta, taus, vis, ks=None):
+    def predict_factors(self, theta, taus, vis, ks=None, member=None):
+        """Factors from one member's network, or from the members' mean (member None)."""
         ks = self.ks if ks is None else np.asarray(ks, dtype=np.float64)
         X = self.features(theta, taus, ks)
-        G = ((self.net.infer(X).astype(np.float64) * self.scale + self.mean) * self.envelope(X[:, 6])).reshape(len(ks), len(taus), 7)
+        nets = self.nets if member is None else [self.nets[member]]
+        Z = np.mean([net.infer(X).astype(np.float64) for net in nets], axis=0)
+        G = ((Z * self.scale + self.mean) * self.envelope(X[:, 6])).reshape(len(ks), len(taus), 7)
         return self.from_targets(G, ks, vis)
 
-    def predict_sources(self, theta, taus, vis, ks=None):
+    def predict_sources(self, theta, taus, vis, ks=None, member=None):
         ks = self.ks if ks is None else np.asarray(ks, dtype=np.float64)
-        return self.sources(self.predict_factors(theta, taus, vis, ks), ks, taus, vis)
+        return self.sources(self.predict_factors(theta, taus, vis, ks, member), ks, taus, vis)
 
     def save(self, path):
-        self.net.save(path)
+        """Weights of every member (path, path.1, ...) and the normalisation (path.norm.npz)."""
+        for m, net in enumerate(self.nets):
+            net.save(path if m == 0 else f"{path}.{m}")
         np.savez(str(path) + ".norm.npz", mean=self.mean, scale=self.scale, env_lk=self.env_lk, env_la=self.env_la, ks=self.ks,
                  ntau=self.ntau)
 
@@ -357,28 +375,57 @@ class SourceSurrogate:
         ref = run(self.sources(F_true, kprobe, taus, vis))
         return self.cl_error(run(self.predict_sources(theta, taus, vis, kprobe)), ref)
 
-    def spectra(self, thetas, jl, ls_out, kinterp, modes=("TT", "TE", "EE"), tol=1e-3, kprobe=None, fallback=True):
-        """C_ℓ (D_ℓ) for each θ: surrogate sources through the line-of-sight pipeline, or the solver
-        for cosmologies whose held-out error estimate (probe_error, relative D_ℓ) exceeds tol.
-        fallback=False: the surrogate alone (no probe modes, error estimates NaN).  Returns
-        (Dl [ncos][nl][nmodes], error estimates, fallback mask)."""
-        from . import CosmologyProblem, spectrum_cmb
-        if fallback:
+    def spectra(self, thetas, jl, ls_out, kinterp, modes=("TT", "TE", "EE"), tol=1e-3, kprobe=None, fallback=True,
+                estimator="ensemble", return_timings=False):
+        """C_ℓ (D_ℓ) for each θ from the surrogate's sources through the line-of-sight pipeline; the
+        cosmologies whose error estimate (relative D_ℓ, the metric of tol) is above tol or not a number
+        are recomputed by the solver, all of their modes in one perturbation launch.
+
+        estimator "ensemble" (needs two members): D_ℓ of the first member's sources against D_ℓ of
+        the members' mean, doubled (≈ the members' disagreement), no mode solved; "probe": D_ℓ from
+        the surrogate's and the solver's sources at 48 probe modes.  fallback=False: the surrogate
+        alone (no estimate, errors NaN).  Returns (Dl [ncos][nl][nmodes], error estimates, fallback
+        mask) and, with return_timings, a dict of phase wall times (s)."""
+        import time
+        from . import solvept, spectrum_cmb
+        tm = {}
+        t0 = time.perf_counter()
+        if fallback and estimator == "probe":
             kprobe = self.probe_kgrid() if kprobe is None else np.asarray(kprobe)
             Fp, taus, vis, prob = self.solve_factors(thetas, ks=kprobe)
-            errs = np.array([self.probe_error(t, taus[c], vis[c], Fp[c], kprobe, prob, c, jl, ls_out) for c, t in enumerate(thetas)])
-            fb = needs_solver(errs, tol)
-        else:  # surrogate only: backgrounds, network, line of sight; no mode is solved
+        else:
             taus, vis, prob = self.backgrounds(thetas)
-            errs = np.full(len(thetas), np.nan)
-            fb = np.zeros(len(thetas), dtype=bool)
-        out = []
+
+        def pipe(c, src):
+            return spectrum_cmb(list(modes), prob, jl, ls_out, kinterp=kinterp, taus=taus[c], cosmo=c, normalization="Dl",
+                                sources=src)
+
+        tm["backgrounds"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        out, errs = [], np.full(len(thetas), np.nan)
         for c, t in enumerate(thetas):
-            if fb[c]:
-                p1 = CosmologyProblem(self.M, box_params(t))
-                out.append(spectrum_cmb(list(modes), p1, jl, ls_out, kinterp=kinterp, taus=taus[c], normalization="Dl"))
-            else:
-                src = self.predict_sources(t, taus[c], vis[c], ks=kinterp.xs)
-                out.append(spectrum_cmb(list(modes), prob, jl, ls_out, kinterp=kinterp, taus=taus[c], cosmo=c, normalization="Dl",
-                                        sources=src))
-        return np.stack(out), errs, fb
+            D = pipe(c, self.predict_sources(t, taus[c], vis[c], ks=kinterp.xs))
+            if fallback and estimator == "ensemble":
+                if len(self.nets) < 2:
+                    raise ValueError("the ensemble estimate needs a surrogate with two or more members")
+                errs[c] = 2 * self.cl_error(pipe(c, self.predict_sources(t, taus[c], vis[c], ks=kinterp.xs, member=0)), D)
+            elif fallback:
+                errs[c] = self.probe_error(t, taus[c], vis[c], Fp[c], kprobe, prob, c, jl, ls_out)
+            out.append(D)
+        tm["surrogate"] = time.perf_counter() - t0
+        fb = needs_solver(errs, tol) if fallback else np.zeros(len(thetas), dtype=bool)
+        t0 = time.perf_counter()
+        flagged = np.flatnonzero(fb)
+        if len(flagged):
+            # every flagged cosmology's modes in one launch, then each through the same pipeline
+            xs = np.asarray(kinterp.xs, dtype=np.float64)
+            src, st, _ = solvept(prob, np.tile(xs, len(flagged)), prob.opts.tau_ini, saveat=taus, output="sources",
+                                 cosmo=np.repeat(flagged, len(xs)))
+            if np.any(st != 0):
+                raise L.SbzError(f"{int(np.count_nonzero(st))} fallback modes failed")
+            src = src.reshape(len(flagged), len(xs), taus.shape[1], 3)
+            for j, c in enumerate(flagged):
+                out[c] = pipe(c, src[j])
+        tm["fallback"] = time.perf_counter() - t0
+        res = (np.stack(out), errs, fb)
+        return res + (tm,) if return_timings else res
