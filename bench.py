@@ -35,6 +35,12 @@ PARAMS = dict(h=H_PLANCK, Omega_c=0.12 / H_PLANCK**2, Omega_b=0.022 / H_PLANCK**
 MODEL = dict(lmax_gamma=30, lmax_nu=10, lmax_h=10, nx=5)
 NK, NTAU, LMAX = 1000, 2000, 2500
 METRIC = "k-mode solves/s (cosmologies/s) at <=1e-4 rel C_l err"
+# Lazy-refinement threshold of the timed configuration: the later stages of a step skip their FP64
+# refinement when stage 1's first correction is below 1e-2 of the error weights.  Measured on this
+# workload at the tolerances below: C_l 7.4e-6 from the all-FP64 solver, 1.5e-5 from a converged
+# solution, 2.01 s per spectrum (2.90 s at 1e-4, 2.26 s at 1e-3).  The library default (1e-5) keeps
+# pointwise sources at the fully refined accuracy; the accuracy field of every run checks the C_l.
+REFINE_SKIP_CL = 1e-2
 # Integrator tolerances of the timed configuration.  The reference's defaults (rtol = atol = 1e-5,
 # src/solve.jl:383) leave the low-l C_l about 1e-2 from a converged solution, and two integrations
 # at those settings (mixed against FP64, GPU against the oracle) can end up 1e-3 apart.  The low-l
@@ -143,7 +149,7 @@ def run_ours(args):
     from symboltz import replicas as R
     rank, world = R.init("nccl")  # replicas: each rank runs the whole workload, no data-path collective
     M = S.ΛCDM(lmax_gamma=MODEL["lmax_gamma"], lmax_nu=MODEL["lmax_nu"], lmax_h=MODEL["lmax_h"], nx=MODEL["nx"])
-    prob = S.CosmologyProblem(M, PARAMS, precision=args.precision, pt_rtol=PT_RTOL, pt_atol=PT_ATOL)
+    prob = S.CosmologyProblem(M, PARAMS, precision=args.precision, refine_skip=REFINE_SKIP_CL, pt_rtol=PT_RTOL, pt_atol=PT_ATOL)
     ks, taus, ls = workload_grids(S, prob)
     jl = S.SphericalBesselCache(ls)
     kinterp = S.CubicSplineInterpolator(ks, f=np.log)
@@ -229,7 +235,7 @@ def run_ours(args):
         "config": {"workload": "LCDM+massive-nu, l_gamma=30, 1000 k log 1e-5..5 h/Mpc, 2000 tau, TT/TE/EE to l=2500",
                    "n_state": prob.nstate, "nk": NK, "ntau": NTAU, "nl_sampled": int(len(ls)), "nk_fine": nk_fine,
                    "precision": args.precision, "pt_rtol": prob.opts.pt_rtol, "pt_atol": prob.opts.pt_atol,
-                   "refinement": "stage 1 of each step (library default)",
+                   "refine_skip": REFINE_SKIP_CL,
                    "l2": "flushed (256 MB write) between steps"},
         "cosmologies_per_s": round(world * K / (dev / 1e3), 4),
         "e2e": {"value": round(e2e_v, 2), "unit": "k-modes/s", "cosmologies_per_s": round(world * K / (e2e / 1e3), 4),
@@ -386,92 +392,156 @@ def mlp_step_bytes(batch=65536, nin_pad=64, width=512, nhidden=4, nout_pad=64, n
 
 
 def run_surrogate(args):
-    """Learned part: training data from the GPU solver (scrambled-Sobol box points; perturbation
-    factors on 400 k × 500 τ), training with the library's BF16 tcgen05 kernels, then C_l (D_l, TT/TE/EE
-    to l = 2500) of held-out cosmologies through surrogate + solver fallback, compared with the
-    all-FP64 solver; cosmologies/s of that path against the plain (mixed-precision) solver path."""
+    """Learned part end to end (cfg4 training, cfg5 mixed workload).
+
+    Training: scrambled-Sobol cosmologies of the box, solved in shards of 64 by the batched GPU
+    solver at the workload's tolerances (perturbation factors on 400 k over 1e-4..0.5 h/Mpc × 500 τ),
+    a random subset of each cosmology's points streamed into a flat SBZTRN01 training-set file, two
+    MLP members (8 → 4×512 SiLU → 7, BF16 tcgen05 GEMMs, FP32 accumulation, Adam, batch 65536)
+    trained from it; a P(k) surrogate (θ, log k → ln Δ_m², 1e-4..10 h/Mpc) trained on the solver's
+    Δ_m.  Held-out accuracy: D_l TT/TE/EE to l = 2500 of held-out cosmologies against the all-FP64
+    solver on the same grids, the surrogate alone and with fallback.  Mixed workload: cosmologies
+    drawn uniformly from the box, D_l to l = 3000 and P(k) from the surrogates, the cosmologies whose
+    ensemble error estimate exceeds the tolerance recomputed by the mixed-precision solver (all of
+    them in one launch), cosmologies/s against the plain solver path, fallback rate, and the error
+    of a sample against the all-FP64 solver."""
     import torch
     import symboltz as S
     from symboltz import surrogate as SG
     assert torch.cuda.is_available(), "bench needs a GPU"
     M = S.ΛCDM(lmax_gamma=MODEL["lmax_gamma"], lmax_nu=MODEL["lmax_nu"], lmax_h=MODEL["lmax_h"], nx=MODEL["nx"])
     ks = S.k_from_hMpc(S.loggrid(1e-4, 0.5, length=400))
-    sur = SG.SourceSurrogate(M, ks, ntau=500, width=512, nhidden=4, batch=65536, seed=0)
+    sur = SG.SourceSurrogate(M, ks, ntau=500, width=512, nhidden=4, batch=65536, seed=0, members=2, pt_rtol=PT_RTOL, pt_atol=PT_ATOL)
+    rng = np.random.default_rng(0)
+    # ---- training data, streamed shard by shard into a flat training-set file
+    path = os.path.join(args.workdir, "sbz_train.sbztrn")
+    if os.path.exists(path):
+        os.remove(path)
+    train = SG.sample_box(args.train_cosmologies, seed=0, sobol=True)
     t0 = time.perf_counter()
-    X, Y, _ = sur.dataset(SG.sample_box(args.train_cosmologies, seed=0, sobol=True))
+    keep = args.points_per_cosmology
+    for s0 in range(0, len(train), 64):
+        th = train[s0:s0 + 64]
+        F, taus, vis, _ = sur.solve_factors(th)
+        for c, t in enumerate(th):
+            X = sur.features(t, taus[c])
+            Y = sur.to_targets(F[c], ks, vis[c]).reshape(-1, 7)
+            idx = rng.choice(len(X), size=min(keep, len(X)), replace=False)
+            SG.write_training_set(path, X[idx], Y[idx])
     t_data = time.perf_counter() - t0
-    losses, steps, t_train = [], 0, 0.0
-    sur.fit(X, Y, steps=1, lr=1e-3)
-    while t_train < args.train_seconds:
-        t1 = time.perf_counter()
-        frac = t_train / args.train_seconds
-        losses.append(sur.net.train(200, 1e-3 * (1e-2) ** frac))
-        t_train += time.perf_counter() - t1
-        steps += 200
+    nin, nout, nrows = SG.training_set_info(path)
+    X, Y = SG.read_training_set(path)
+    # ---- training both members (fit sets the envelope and standardisation from the same data)
+    step_s = 1.2e-3
+    steps = max(200, int(args.train_seconds / len(sur.nets) / step_s))
+    t0 = time.perf_counter()
+    losses = sur.fit(X, Y, steps=steps, lr=1e-3, lr_final=1e-5)
+    t_train = time.perf_counter() - t0
     mse_train = sur.mse(X[:: max(1, len(X) // 2_000_000)], Y[:: max(1, len(X) // 2_000_000)])
     del X, Y
-    flops_step = 3 * 2 * 65536 * (64 * 512 + 3 * 512 * 512 + 512 * 64)  # forward + 2 backward GEMM sets
-    test = SG.sample_box(args.test_cosmologies, seed=1)
+    flops_step = 3 * 2 * 65536 * (64 * 512 + 3 * 512 * 512 + 512 * 64)
+    # P(k) surrogate, trained on the solver's Δ_m at the reference's default tolerances
+    kpk = S.k_from_hMpc(S.loggrid(1e-4, 10.0, length=128))
+    msur = SG.MatterSurrogate(M, kpk, seed=1)
+    t0 = time.perf_counter()
+    Xp, Yp = [], []
+    for s0 in range(0, args.pk_train_cosmologies, 128):
+        xp, yp = msur.dataset(train[s0:min(s0 + 128, args.pk_train_cosmologies)])
+        Xp.append(xp); Yp.append(yp)
+    msur.fit(np.concatenate(Xp), np.concatenate(Yp).astype(np.float32), steps=4000, lr=1e-3, lr_final=1e-5)
+    t_pk = time.perf_counter() - t0
+    # ---- held-out accuracy against the all-FP64 solver (same grids and tolerances)
     ls = np.unique(np.round(np.exp(np.linspace(np.log(2), np.log(LMAX), 200))).astype(np.int32))
+    lall = np.arange(2, LMAX + 1)
     jl = S.SphericalBesselCache(ls)
     kin = S.CubicSplineInterpolator(ks, f=np.log)
-    lall = np.arange(2, LMAX + 1)
-    # accuracy reference: the all-FP64 solver on the same grids
-    _, taus, _, _ = sur.solve_factors(test[:1])
-    ref64, t_solver = [], 0.0
-    for th in test:
-        p64 = S.CosmologyProblem(M, SG.box_params(th), precision="fp64")
-        bg = p64.solvebg()
-        tt = SG.cmb_taus(bg.t(0), bg.tau0[0], sur.ntau)
-        ref64.append(S.spectrum_cmb(["TT", "TE", "EE"], p64, jl, lall, kinterp=kin, taus=tt, normalization="Dl"))
-        pm = S.CosmologyProblem(M, SG.box_params(th))
-        t1 = time.perf_counter()
-        bgm = pm.solvebg()
-        S.spectrum_cmb(["TT", "TE", "EE"], pm, jl, lall, kinterp=kin, taus=SG.cmb_taus(bgm.t(0), bgm.tau0[0], sur.ntau), normalization="Dl")
-        t_solver += time.perf_counter() - t1
-    ref64 = np.stack(ref64)
-    t1 = time.perf_counter()
+    test = SG.sample_box(args.test_cosmologies, seed=1)
+
+    def solver_spectra(thetas, precision):
+        prob = S.CosmologyProblem(M, [SG.box_params(t) for t in thetas], precision=precision, pt_rtol=PT_RTOL, pt_atol=PT_ATOL)
+        bg = prob.solvebg()
+        taus = np.stack([SG.cmb_taus(bg.t(c), bg.tau0[c], sur.ntau) for c in range(len(thetas))])
+        src, st, _ = S.solvept(prob, np.tile(ks, len(thetas)), prob.opts.tau_ini, saveat=taus, output="sources",
+                               cosmo=np.repeat(np.arange(len(thetas)), len(ks)))
+        src = src.reshape(len(thetas), len(ks), sur.ntau, 3)
+        return np.stack([S.spectrum_cmb(["TT", "TE", "EE"], prob, jl, lall, kinterp=kin, taus=taus[c], cosmo=c, normalization="Dl",
+                                        sources=src[c]) for c in range(len(thetas))])
+
+    def rel_max(D, R):
+        den = [np.abs(R[..., 0]), np.sqrt(np.abs(R[..., 0] * R[..., 2])), np.abs(R[..., 2])]
+        return np.stack([np.max(np.abs(D[..., i] - R[..., i]) / den[i], axis=-1) for i in range(3)], axis=-1).max(axis=-1)
+
+    ref64 = solver_spectra(test, "fp64")
+    t0 = time.perf_counter()
+    solver_spectra(test, "mixed")
+    t_solver = time.perf_counter() - t0
+    t0 = time.perf_counter()
     Dl, errs, fb = sur.spectra(test, jl, lall, kin, tol=args.surrogate_tol)
-    t_sur = time.perf_counter() - t1
-    den = [np.abs(ref64[..., 0]), np.sqrt(np.abs(ref64[..., 0] * ref64[..., 2])), np.abs(ref64[..., 2])]
-    rel = np.stack([np.max(np.abs(Dl[..., i] - ref64[..., i]) / den[i], axis=1) for i in range(3)], axis=1)  # [cosmo][mode]
-    t1 = time.perf_counter()
+    t_sur = time.perf_counter() - t0
+    t0 = time.perf_counter()
     Dl_raw, _, _ = sur.spectra(test, jl, lall, kin, fallback=False)
-    t_raw = time.perf_counter() - t1
-    rel_raw = np.stack([np.max(np.abs(Dl_raw[..., i] - ref64[..., i]) / den[i], axis=1) for i in range(3)], axis=1)
+    t_raw = time.perf_counter() - t0
+    rel, rel_raw = rel_max(Dl, ref64), rel_max(Dl_raw, ref64)
     n = len(test)
     line = {"metric": "cosmologies/s (surrogate + fallback vs solver)", "value": round(n / t_sur, 3), "unit": "cosmologies/s",
-            "workload": f"{n} held-out cosmologies from the box, C_l TT/TE/EE to l={LMAX} (D_l), 400 k x 500 tau",
+            "workload": f"{n} held-out cosmologies from the box, D_l TT/TE/EE to l={LMAX}, 400 k x 500 tau, rtol {PT_RTOL:g} atol {PT_ATOL:g}",
             "solver_cosmologies_per_s": round(n / t_solver, 3), "speedup": round(t_solver / t_sur, 3),
-            "fallback_rate": float(fb.mean()), "tol_probe": args.surrogate_tol,
-            "probe_error": {"median": float(np.median(errs)), "max": float(np.max(errs))},
-            "cl_max_rel_vs_fp64": {"with_fallback": {"median": float(np.median(rel.max(axis=1))), "max": float(rel.max())},
-                                   "surrogate_only": {"median": float(np.median(rel_raw.max(axis=1))), "max": float(rel_raw.max()),
-                                                      "median_by_spectrum": dict(zip(("TT", "TE", "EE"),
-                                                                                     np.median(rel_raw, axis=0).round(6).tolist()))}},
-            "surrogate_only": {"cosmologies_per_s": round(n / t_raw, 3), "speedup_vs_solver": round(t_solver / t_raw, 2),
-                               "cl_max_rel_median": float(np.median(rel_raw.max(axis=1))),
-                               "note": "backgrounds + network + line of sight, no mode solved: what the network gains in speed, at its accuracy"},
-            "estimate_vs_true_surrogate_error": [[round(float(e), 6), round(float(t), 6)] for e, t in zip(errs, rel_raw.max(axis=1))],
-            "training": {"cosmologies": args.train_cosmologies, "samples": int(args.train_cosmologies * len(ks) * sur.ntau),
-                         "data_s": round(t_data, 2), "steps": steps, "train_s": round(t_train, 2),
-                         "tflops": round(steps * flops_step / t_train / 1e12, 1), "batch": 65536,
-                         "loss_first_last": [losses[0], losses[-1]], "mse_train_standardised": mse_train},
-            "model": "MLP 8 -> 4x512 SiLU -> 7 (perturbation factors), BF16 tcgen05 GEMMs, FP32 accumulate, Adam"}
+            "fallback_rate": float(fb.mean()), "tol": args.surrogate_tol,
+            "cl_max_rel_vs_fp64": {"with_fallback": {"median": float(np.median(rel)), "max": float(rel.max())},
+                                   "surrogate_only": {"median": float(np.median(rel_raw)), "max": float(rel_raw.max()),
+                                                      "p90": float(np.quantile(rel_raw, 0.9))}},
+            "surrogate_only": {"cosmologies_per_s": round(n / t_raw, 3), "speedup_vs_solver": round(t_solver / t_raw, 2)},
+            "estimate_vs_true": {"median_ratio": float(np.median(errs / rel_raw)),
+                                 "pairs": [[round(float(e), 6), round(float(t), 6)] for e, t in zip(errs[:16], rel_raw[:16])]},
+            "training": {"cosmologies": len(train), "rows": int(nrows), "points_per_cosmology": keep, "file": "SBZTRN01",
+                         "data_s": round(t_data, 2), "steps_per_member": steps, "members": len(sur.nets), "train_s": round(t_train, 2),
+                         "tflops": round(len(sur.nets) * steps * flops_step / t_train / 1e12, 1), "batch": 65536,
+                         "loss_first_last": [losses[0][0], losses[0][-1]], "mse_train_standardised": mse_train,
+                         "pk_surrogate": {"cosmologies": args.pk_train_cosmologies, "k": len(kpk), "s": round(t_pk, 2)}},
+            "model": "MLP 8 -> 4x512 SiLU -> 7 (perturbation factors) x 2 members, BF16 tcgen05 GEMMs, FP32 accumulate, Adam"}
     peaks = measured_peaks()
-    step_s = t_train / steps
     nbytes = mlp_step_bytes()
+    sps = t_train / (len(sur.nets) * steps)
     line["training"]["roofline"] = {
-        "bound": "hbm", "unit": "GB/s", "achieved": round(nbytes / step_s / 1e9, 1), "peak": peaks.get("hbm_gbs"),
-        "frac": round(nbytes / step_s / 1e9 / peaks["hbm_gbs"], 4) if peaks.get("hbm_gbs") else None, "traffic": None,
-        "bytes_per_step": nbytes, "ms_per_step": round(step_s * 1e3, 4),
-        "tensor_tflops": round(steps * flops_step / t_train / 1e12, 1), "tensor_peak_sustained": peaks.get("bf16_tflops_sustained"),
-        "tensor_frac": round(steps * flops_step / t_train / 1e12 / peaks["bf16_tflops_sustained"], 4) if peaks.get("bf16_tflops_sustained") else None}
+        "bound": "hbm", "unit": "GB/s", "achieved": round(nbytes / sps / 1e9, 1), "peak": peaks.get("hbm_gbs"),
+        "frac": round(nbytes / sps / 1e9 / peaks["hbm_gbs"], 4) if peaks.get("hbm_gbs") else None, "traffic": None,
+        "bytes_per_step": nbytes, "ms_per_step": round(sps * 1e3, 4),
+        "tensor_tflops": round(flops_step / sps / 1e12, 1), "tensor_peak_sustained": peaks.get("bf16_tflops_sustained"),
+        "tensor_frac": round(flops_step / sps / 1e12 / peaks["bf16_tflops_sustained"], 4) if peaks.get("bf16_tflops_sustained") else None}
+    # ---- mixed workload: D_l to l = 3000 and P(k) from the surrogates, flagged cosmologies to the solver
+    if args.mixed_cosmologies > 0:
+        lmix = np.arange(2, 3001)
+        lsm = np.unique(np.round(np.exp(np.linspace(np.log(2), np.log(3000), 200))).astype(np.int32))
+        jlm = S.SphericalBesselCache(lsm)
+        mix = SG.sample_box(args.mixed_cosmologies, seed=2)
+        t0 = time.perf_counter()
+        Dm, em, fm, tm = sur.spectra(mix, jlm, lmix, kin, tol=args.surrogate_tol, return_timings=True)
+        Pm, epm, fpm = msur.spectra(mix, tol=args.surrogate_tol)
+        t_mix = time.perf_counter() - t0
+        nchk = min(args.mixed_check, len(mix))
+        prob = S.CosmologyProblem(M, [SG.box_params(t) for t in mix[:nchk]], precision="fp64", pt_rtol=PT_RTOL, pt_atol=PT_ATOL)
+        bg = prob.solvebg()
+        taus = np.stack([SG.cmb_taus(bg.t(c), bg.tau0[c], sur.ntau) for c in range(nchk)])
+        src, _, _ = S.solvept(prob, np.tile(ks, nchk), prob.opts.tau_ini, saveat=taus, output="sources",
+                              cosmo=np.repeat(np.arange(nchk), len(ks)))
+        src = src.reshape(nchk, len(ks), sur.ntau, 3)
+        Dref = np.stack([S.spectrum_cmb(["TT", "TE", "EE"], prob, jlm, lmix, kinterp=kin, taus=taus[c], cosmo=c, normalization="Dl",
+                                        sources=src[c]) for c in range(nchk)])
+        mref = SG.MatterSurrogate(M, kpk, members=1, pt_rtol=PT_RTOL, pt_atol=PT_ATOL)
+        Pref = np.stack([S.spectrum_primordial(kpk, prob, c) for c in range(nchk)]) * mref.solve(mix[:nchk], prob=prob) ** 2
+        rc = rel_max(Dm[:nchk], Dref)
+        rp = np.max(np.abs(Pm[:nchk] / Pref - 1), axis=1)
+        line["mixed_workload"] = {
+            "cosmologies": len(mix), "cosmologies_per_s": round(len(mix) / t_mix, 3), "seconds": round(t_mix, 2),
+            "fallback_rate_cl": float(fm.mean()), "fallback_rate_pk": float(fpm.mean()), "phases_s": {k: round(v, 2) for k, v in tm.items()},
+            "checked_vs_fp64": nchk, "cl_max_rel_l2_3000": {"median": float(np.median(rc)), "max": float(rc.max())},
+            "pk_max_rel_1e-4_10hMpc": {"median": float(np.median(rp)), "max": float(rp.max())},
+            "plain_solver_cosmologies_per_s": round(n / t_solver, 3)}
     print(json.dumps(line), flush=True)
 
 
 def profile_case(args):
-    """Small cases for ncu section captures, at the workload's tolerances.  pt: 64 of the 1000 modes
+    """Small cases for ncu section captures, at the workload's tolerances and refinement threshold.  pt: 64 of the 1000 modes
     (even in log k, the slowest included), sources on 200 times.  los: one spectrum_cmb of the full workload (the line-of-sight
     kernel runs once on the full fine k grid; ~1.5 GB on the device).  mlp: the surrogate's training
     step (8 -> 4x512 -> 7, batch 65536) on 2 M synthetic samples, one eager step, the graph capture
@@ -491,7 +561,7 @@ def profile_case(args):
                               "tflops": round(3 * 2 * 65536 * (64 * 512 + 3 * 512 * 512 + 512 * 64) * args.steps / dt / 1e12, 1)}))
         return
     M = S.ΛCDM(lmax_gamma=MODEL["lmax_gamma"], lmax_nu=MODEL["lmax_nu"], lmax_h=MODEL["lmax_h"], nx=MODEL["nx"])
-    prob = S.CosmologyProblem(M, PARAMS, precision=args.precision, pt_rtol=PT_RTOL, pt_atol=PT_ATOL)
+    prob = S.CosmologyProblem(M, PARAMS, precision=args.precision, refine_skip=REFINE_SKIP_CL, pt_rtol=PT_RTOL, pt_atol=PT_ATOL)
     ks, taus, ls = workload_grids(S, prob)
     if args.profile_case == "pt":
         sel = ks[np.linspace(0, len(ks) - 1, 64).round().astype(int)]
@@ -512,10 +582,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--train-cosmologies", type=int, default=64)
-    ap.add_argument("--train-seconds", type=float, default=120.0)
-    ap.add_argument("--test-cosmologies", type=int, default=16)
+    ap.add_argument("--train-cosmologies", type=int, default=1024)
+    ap.add_argument("--points-per-cosmology", type=int, default=40000)
+    ap.add_argument("--pk-train-cosmologies", type=int, default=512)
+    ap.add_argument("--train-seconds", type=float, default=300.0)
+    ap.add_argument("--test-cosmologies", type=int, default=32)
+    ap.add_argument("--mixed-cosmologies", type=int, default=4096)
+    ap.add_argument("--mixed-check", type=int, default=16)
     ap.add_argument("--surrogate-tol", type=float, default=1e-3)
+    ap.add_argument("--workdir", default=tempfile.gettempdir(), help="where the training-set file is written")
     ap.add_argument("--clocks-log", default=os.path.join(tempfile.gettempdir(), "sbz_bench_clocks.csv"),
                     help="CSV of the nvidia-smi clock samples taken during the timed region")
     ap.add_argument("--workload", choices=("spectrum", "batched", "surrogate"), default="spectrum",

@@ -74,10 +74,12 @@ typedef struct sbz_opts {
   int los_precision;        /* line of sight: SBZ_FP64 or SBZ_MIXED (FP32 interpolation); -1 = as precision */
   double refine_skip;       /* SBZ_MIXED: the later stages (2-8) of a step are refined only when stage 1's
                                first correction is at or above this (error-weight units); stage 1 is always
-                               refined.  0 = refine every stage; < 0 (default) = never refine the later
-                               stages: on the 1000-mode massive-ν spectrum at rtol 1e-6, atol 3e-8 their FP32
-                               solves leave C_l 3.9e-6 from the all-FP64 solver (5.9e-6 with every stage
-                               refined) at 1.99 s against 2.90 s */
+                               refined.  0 = refine every stage; < 0 (default) = 1e-5 for four-warp groups
+                               (sources at the fully refined accuracy) and 0 for narrower ones.  Larger
+                               values trade pointwise source accuracy for speed: 1e-2 keeps the 1000-mode
+                               massive-ν C_l within 7.4e-6 of the all-FP64 solver at rtol 1e-6, atol 3e-8
+                               (2.01 s against 2.90 s at 1e-4), while skipping the later stages' refinement
+                               outright leaves pointwise sources of the ΛCDM(lmax = 5) model 1e-2 off */
 } sbz_opts;
 
 typedef struct sbz_problem sbz_problem;

@@ -1040,8 +1040,8 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         for (int sl = 0; sl < NSL; ++sl) b[sl] = f0[sl] + h * TB::d(0) * ft[sl];
         float c1 = 1e30f;
         stage_solve(g, W, F, CJ, comps, M, k, s, A.refine, scan, isk, b, U[0], &c1);
-        // the later stages share stage 1's W; they are refined only when stage 1's first FP64
-        // correction is at or above refine_skip (error-weight units; the default never refines them)
+        // lazy refinement: the later stages share stage 1's W; they are refined only when stage 1's
+        // first FP64 correction is at or above refine_skip (error-weight units)
         const int rk = (A.refine > 0 && c1 < A.refine_skip) ? 0 : A.refine;
 #pragma unroll
         for (int st = 1; st < TB::S; ++st) {

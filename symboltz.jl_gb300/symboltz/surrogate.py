@@ -429,3 +429,90 @@ class SourceSurrogate:
         tm["fallback"] = time.perf_counter() - t0
         res = (np.stack(out), errs, fb)
         return res + (tm,) if return_timings else res
+
+
+class MatterSurrogate:
+    """P(k) at z = 0 from an MLP of (θ, log k) to ln Δ_m(τ0)² (spectrum_matter's transfer factor,
+    src/observables/fourier.jl:79-101; P = P0 Δ_m²), standardised; like SourceSurrogate it keeps two
+    members and estimates each cosmology's error from their disagreement, and the solver (Δ_m output,
+    one launch for all flagged cosmologies) is its fallback."""
+
+    def __init__(self, M, ks, width=256, nhidden=3, batch=8192, seed=0, members=2, pt_rtol=1e-5, pt_atol=1e-5):
+        self.M, self.ks = M, np.asarray(ks, dtype=np.float64)
+        self.logk = (np.log(self.ks.min()), np.log(self.ks.max()))
+        self.nets = [MLP(7, width, nhidden, 1, batch, seed + 104729 * i) for i in range(max(1, members))]
+        self.pt_rtol, self.pt_atol = pt_rtol, pt_atol
+        self.mean, self.scale = 0.0, 1.0
+
+    def features(self, theta, ks=None):
+        ks = self.ks if ks is None else np.asarray(ks, dtype=np.float64)
+        X = np.empty((len(ks), 7), dtype=np.float32)
+        X[:, :6] = 2 * (np.asarray(theta) - BOX[:, 0]) / (BOX[:, 1] - BOX[:, 0]) - 1
+        X[:, 6] = 2 * (np.log(ks) - self.logk[0]) / (self.logk[1] - self.logk[0]) - 1
+        return X
+
+    def problem(self, thetas):
+        from . import CosmologyProblem
+        prob = CosmologyProblem(self.M, [box_params(t) for t in thetas], pt_rtol=self.pt_rtol, pt_atol=self.pt_atol)
+        if np.any(prob.solvebg().status != 0):
+            raise L.SbzError("background failed for a cosmology of the box")
+        return prob
+
+    def solve(self, thetas, prob=None, which=None):
+        """Δ_m(τ0) [ncos][nk] from the solver: every mode of the cosmologies `which` (default all) in
+        one launch, spectrum_matter's initial times."""
+        from . import solvept
+        prob = self.problem(thetas) if prob is None else prob
+        which = np.arange(len(thetas)) if which is None else np.asarray(which)
+        nk = len(self.ks)
+        dm, st, _ = solvept(prob, np.tile(self.ks, len(which)), lambda k: np.minimum(1e-2 / k, 1e-4), output="delta_m",
+                            cosmo=np.repeat(which, nk))
+        if np.any(st != 0):
+            raise L.SbzError(f"{int(np.count_nonzero(st))} modes failed")
+        return dm.reshape(len(which), nk)
+
+    def dataset(self, thetas):
+        dm = self.solve(thetas)
+        X = np.concatenate([self.features(t) for t in thetas])
+        Y = np.log(dm.reshape(-1, 1) ** 2)
+        return X, Y
+
+    def fit(self, X, Y, steps, lr=1e-3, lr_final=1e-5, chunks=20):
+        self.mean, self.scale = float(Y.mean()), float(Y.std()) + 1e-30
+        Z = ((Y - self.mean) / self.scale).astype(np.float32)
+        losses = []
+        for net in self.nets:
+            net.set_data(X, Z)
+            per, done, lm = max(1, steps // chunks), 0, []
+            while done < steps:
+                n = min(per, steps - done)
+                lm.append(net.train(n, lr * (lr_final / lr) ** (done / max(1, steps))))
+                done += n
+            losses.append(lm)
+        return losses
+
+    def transfer2(self, theta, member=None):
+        """Δ_m² on the k grid from one member or the members' mean (in ln Δ_m²)."""
+        X = self.features(theta)
+        nets = self.nets if member is None else [self.nets[member]]
+        Z = np.mean([net.infer(X).astype(np.float64)[:, 0] for net in nets], axis=0)
+        return np.exp(Z * self.scale + self.mean)
+
+    def spectra(self, thetas, tol=1e-3, fallback=True, prob=None):
+        """P(k) [ncos][nk] at z = 0, surrogate or (estimate above tol or not a number) the solver;
+        returns (P, error estimates, fallback mask)."""
+        from . import spectrum_primordial
+        prob = self.problem(thetas) if prob is None else prob
+        T2 = np.stack([self.transfer2(t) for t in thetas])
+        errs = np.full(len(thetas), np.nan)
+        if fallback:
+            if len(self.nets) < 2:
+                raise ValueError("the ensemble estimate needs two or more members")
+            for c, t in enumerate(thetas):
+                errs[c] = 2 * float(np.max(np.abs(self.transfer2(t, member=0) / T2[c] - 1)))
+        fb = needs_solver(errs, tol) if fallback else np.zeros(len(thetas), dtype=bool)
+        flagged = np.flatnonzero(fb)
+        if len(flagged):
+            T2[flagged] = self.solve(thetas, prob=prob, which=flagged) ** 2
+        P = np.stack([spectrum_primordial(self.ks, prob, c) for c in range(len(thetas))]) * T2
+        return P, errs, fb

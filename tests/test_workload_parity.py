@@ -59,9 +59,10 @@ def oracle_spectrum(S, B):
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_bench_spectrum_matches_oracle(S, B, oracle_spectrum, precision):
     """Every l of TT, TE, EE within 1e-4 of the oracle at the bench's settings (the timed
-    configuration itself: library defaults, mixed precision with stage-1 refinement)."""
+    configuration itself: mixed precision with the bench's lazy-refinement threshold)."""
     o = oracle_spectrum
-    prob = S.CosmologyProblem(o["M"], B.PARAMS, precision=precision, pt_rtol=B.PT_RTOL, pt_atol=B.PT_ATOL)
+    skip = B.REFINE_SKIP_CL if precision == "mixed" else None
+    prob = S.CosmologyProblem(o["M"], B.PARAMS, precision=precision, refine_skip=skip, pt_rtol=B.PT_RTOL, pt_atol=B.PT_ATOL)
     jl = S.SphericalBesselCache(o["ls"])
     kin = S.CubicSplineInterpolator(o["ks"], f=np.log)
     Dl, st = S.spectrum_cmb(["TT", "TE", "EE"], prob, jl, o["lall"], kinterp=kin, taus=o["taus"], return_status=True,
