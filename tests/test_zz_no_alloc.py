@@ -4,6 +4,7 @@ against sbz_cl_integrate, through the C-ABI.
 Collected last on purpose: it must give the same answer whether it runs alone in a fresh process
 or after every other test has used the library on the same device."""
 import ctypes as C
+import gc
 
 import numpy as np
 import pytest
@@ -93,14 +94,18 @@ def test_noalloc_warm_calls_take_no_device_memory():
             C.c_void_p(out.data_ptr()), C.c_void_p(stream.cuda_stream))
     assert L.sbz_cl_integrate_noalloc(*args) == 0, L.sbz_last_error()
     torch.cuda.synchronize()
+    # objects of earlier tests still waiting for the garbage collector free their device buffers
+    # when it runs; let it run now, so the readings below only see this entry
+    gc.collect()
+    torch.cuda.synchronize()
     free0, _ = torch.cuda.mem_get_info()
     reserved0 = torch.cuda.memory_reserved()
     for _ in range(20):
         assert L.sbz_cl_integrate_noalloc(*args) == 0, L.sbz_last_error()
         free_mid, _ = torch.cuda.mem_get_info()
-        assert free_mid == free0
+        assert free_mid >= free0, (free_mid, free0)  # an allocation inside the call would lower it
     torch.cuda.synchronize()
-    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.mem_get_info()[0] >= free0
     assert torch.cuda.memory_reserved() == reserved0
     np.testing.assert_allclose(out.cpu().numpy(), _reference(L, ks, P0, ThA, ThB), rtol=RTOL,
                                atol=1e-12 * float(torch.max(torch.abs(out))))
