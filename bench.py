@@ -344,7 +344,8 @@ def run_batched(args):
     ti = lambda k: np.minimum(1e-2 / k, 1e-4)  # noqa: E731  (spectrum_matter's rule, fourier.jl:76-81)
     res, chosen = {}, {}
     for prec in ("mixed", "fp64"):  # the FP64 run uses the launch shape tuned for the mixed run
-        prob = S.CosmologyProblem(M, pars, precision=prec, **chosen)
+        skip = REFINE_SKIP_CL if prec == "mixed" else None
+        prob = S.CosmologyProblem(M, pars, precision=prec, pt_rtol=PT_RTOL, pt_atol=PT_ATOL, refine_skip=skip, **chosen)
         t0 = time.perf_counter()
         bg = prob.solvebg()
         t_bg = time.perf_counter() - t0
@@ -360,6 +361,7 @@ def run_batched(args):
             times.append(time.perf_counter() - t0)
         res[prec] = dict(s=min(times), dm=dm, failed=int(np.count_nonzero(st)), steps=int(stp.sum()), bg_s=t_bg, tune=tune)
     rel = np.abs(res["mixed"]["dm"] ** 2 - res["fp64"]["dm"] ** 2) / res["fp64"]["dm"] ** 2
+    hi = ks >= S.k_from_hMpc(1e-4)
     n = len(ks)
     line = {"metric": "k-mode solves/s (batched P(k))", "value": round(n / res["mixed"]["s"], 2), "unit": "k-modes/s",
             "workload": f"batched: {len(pars)} cosmologies from the parameter box, U{{200..800}} k each ({n} modes), P(k) at z=0",
@@ -370,7 +372,8 @@ def run_batched(args):
             "fp64": {"s": round(res["fp64"]["s"], 3), "kmodes_per_s": round(n / res["fp64"]["s"], 1), "failed": res["fp64"]["failed"],
                      "steps": res["fp64"]["steps"]},
             "speedup_mixed_over_fp64": round(res["fp64"]["s"] / res["mixed"]["s"], 3),
-            "pk_rel_mixed_vs_fp64": {"max": float(rel.max()), "median": float(np.median(rel))},
+            "pk_rel_mixed_vs_fp64": {"max": float(rel.max()), "median": float(np.median(rel)), "max_k_ge_1e-4_hMpc": float(rel[hi].max())},
+            "tolerances": {"pt_rtol": PT_RTOL, "pt_atol": PT_ATOL, "refine_skip_mixed": REFINE_SKIP_CL},
             "background_s": round(res["mixed"]["bg_s"], 3)}
     print(json.dumps(line), flush=True)
 
@@ -414,6 +417,7 @@ def run_surrogate(args):
     sur = SG.SourceSurrogate(M, ks, ntau=500, width=512, nhidden=4, batch=65536, seed=0, members=2, pt_rtol=PT_RTOL, pt_atol=PT_ATOL)
     rng = np.random.default_rng(0)
     # ---- training data, streamed shard by shard into a flat training-set file
+    os.makedirs(args.workdir, exist_ok=True)
     path = os.path.join(args.workdir, "sbz_train.sbztrn")
     if os.path.exists(path):
         os.remove(path)

@@ -69,7 +69,7 @@ typedef struct sbz_opts {
                                once a correction is < 1e-3 of the error tolerance; default 3 */
   int table_points;         /* background coefficient table nodes, default 8192 */
   int warps_per_block;      /* warps per thread block (≤ 4); 0 = 4 */
-  int warps_per_mode;       /* warps integrating one mode: 1, 2 or 4; 0 = chosen from the number of modes */
+  int warps_per_mode;       /* warps integrating one mode: 1, 2, 4 or 8; 0 = chosen from the number of modes */
   int blocks_per_sm;        /* resident thread blocks per SM for the perturbation kernel; 0 = chosen */
   int los_precision;        /* line of sight: SBZ_FP64 or SBZ_MIXED (FP32 interpolation); -1 = as precision */
   double refine_skip;       /* SBZ_MIXED: the later stages (2-8) of a step are refined only when stage 1's
@@ -185,11 +185,11 @@ int sbz_problem_timings(const sbz_problem* pb, double* ms8);
 
 /* No counterpart in the reference (its solvept threads over k on the CPU).  Autotuner for the
  * perturbation kernel's launch shape: times the candidates (warps per mode, blocks per SM) =
- * (1,0) (2,0) (2,2) (4,1) (4,2) (4,3) on a k-stratified sample of the given modes (an eighth of
+ * (1,0) (2,0) (2,2) (4,1) (4,2) (4,3) (8,1) on a k-stratified sample of the given modes (an eighth of
  * them above 2048 modes, all of them otherwise), stores the fastest in the problem's options and
  * returns it in best[2]; ms[SBZ_TUNE_CANDIDATES] receives the candidates' kernel times (may be
  * NULL).  Arguments as sbz_solve_pt. */
-#define SBZ_TUNE_CANDIDATES 6
+#define SBZ_TUNE_CANDIDATES 7
 int sbz_autotune_pt(sbz_problem* pb, int nk, const int* cosmo, const double* ks, const double* tau_ini, int ntau,
                     const double* taus, int output, int* best, double* ms);
 

@@ -533,7 +533,7 @@ int sbz_autotune_pt(sbz_problem* pb, int nk, const int* cosmo, const double* ks,
   if (ntau > 0) SBZ_CUDA(cudaMemcpyAsync(pb->d_taus.p, taus, sizeof(double) * ntau * pb->ncosmo, cudaMemcpyHostToDevice, s));
   int r;
   if ((r = ensure_events(pb)) != SBZ_OK) return r;
-  const int cand[SBZ_TUNE_CANDIDATES][2] = {{1, 0}, {2, 0}, {2, 2}, {4, 1}, {4, 2}, {4, 3}};
+  const int cand[SBZ_TUNE_CANDIDATES][2] = {{1, 0}, {2, 0}, {2, 2}, {4, 1}, {4, 2}, {4, 3}, {8, 1}};
   const int keep_nw = pb->opts.warps_per_mode, keep_bps = pb->opts.blocks_per_sm;
   double best_ms = 1e300;
   int bi = 0;

@@ -1,4 +1,4 @@
-// FP32 factorisation + FP64 refinement instantiations of the perturbation kernel, 2 and 4 warp(s) per mode.
+// FP32 factorisation + FP64 refinement instantiations of the perturbation kernel, 2, 4 and 8 warps per mode.
 #include "sbz_pt_impl.cuh"
 
 namespace sbz {
@@ -17,6 +17,11 @@ int pt_launch_f32_w2_w4(const PtArgs& A, int nw, int warps_per_block, int blocks
       switch ((A.model_n + 127) / 128) {
       case 1: return launch_nw<4, 1, float>(A, warps_per_block, blocks_per_sm, num_sms, stream);
       case 2: return launch_nw<4, 2, float>(A, warps_per_block, blocks_per_sm, num_sms, stream);
+        default: return SBZ_ERR_ARG;
+      }
+    case 8:
+      switch ((A.model_n + 255) / 256) {
+      case 1: return launch_nw<8, 1, float>(A, warps_per_block, blocks_per_sm, num_sms, stream);
         default: return SBZ_ERR_ARG;
       }
     default: return SBZ_ERR_ARG;

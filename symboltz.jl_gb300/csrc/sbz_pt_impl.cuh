@@ -1197,10 +1197,11 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
 }
 
 // Register budget: four-warp groups run at most two per SM (tail-bound spectra), so they may use up
-// to 256 registers per thread and need not spill; narrower groups keep three 128-thread blocks per
-// SM (throughput-bound batches), accepting a few spilled registers for the occupancy.
+// to 256 registers per thread and need not spill; eight-warp groups (one 256-thread block per SM:
+// one mode per SM, two warps per sub-partition) likewise; narrower groups keep three 128-thread
+// blocks per SM (throughput-bound batches), accepting a few spilled registers for the occupancy.
 template <int NW, int NSL, typename ST>
-__global__ void __launch_bounds__(128, NW >= 4 ? 2 : 3) pt_kernel(PtArgs A) {
+__global__ void __launch_bounds__(NW >= 8 ? 256 : 128, NW >= 8 ? 1 : NW >= 4 ? 2 : 3) pt_kernel(PtArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ModelDesc& M = *reinterpret_cast<ModelDesc*>(smem_raw);
   CompDesc* comps = reinterpret_cast<CompDesc*>(smem_raw + ((sizeof(ModelDesc) + 15) & ~size_t(15)));
@@ -1225,7 +1226,7 @@ __global__ void __launch_bounds__(128, NW >= 4 ? 2 : 3) pt_kernel(PtArgs A) {
 template <int NW, int NSL, typename ST>
 int launch_nw(const PtArgs& A, int warps_per_block, int blocks_per_sm, int num_sms, cudaStream_t stream) {
   using Mem = ModeMem<NW, NSL, ST>;
-  const int wpb = warps_per_block < NW ? NW : warps_per_block > 4 ? 4 : warps_per_block;  // ≤ 128 threads
+  const int wpb = warps_per_block < NW ? NW : warps_per_block > 4 ? 4 : warps_per_block;  // ≤ 128 threads, or one 8-warp group
   const int groups = wpb / NW;
   const size_t head = ((sizeof(ModelDesc) + 15) & ~size_t(15)) + (((size_t)A.model_n * sizeof(CompDesc) + 15) & ~size_t(15));
   const size_t smem = head + groups * sizeof(Mem);

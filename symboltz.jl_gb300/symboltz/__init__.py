@@ -240,10 +240,10 @@ def autotune(prob: CosmologyProblem, ks, ptivini=-np.inf, *, saveat=None, output
         taus = np.broadcast_to(taus, (prob.ncosmo, taus.shape[-1])) if taus.ndim == 1 else taus
     taus = L.f64(taus)
     best = L.i32(np.zeros(2))
-    ms = L.f64(np.zeros(6))
+    ms = L.f64(np.zeros(7))
     L.check(L.lib().sbz_autotune_pt(prob._h, nk, L.iptr(cos), L.dptr(ks), L.dptr(ti), taus.shape[1], L.dptr(taus), kind,
                                     L.iptr(best), L.dptr(ms)), "autotune")
-    cands = [(1, 0), (2, 0), (2, 2), (4, 1), (4, 2), (4, 3)]
+    cands = [(1, 0), (2, 0), (2, 2), (4, 1), (4, 2), (4, 3), (8, 1)]
     prob.opts.warps_per_mode, prob.opts.blocks_per_sm = int(best[0]), int(best[1])
     return {"warps_per_mode": int(best[0]), "blocks_per_sm": int(best[1]), "candidates_ms": {c: float(m) for c, m in zip(cands, ms)}}
 
