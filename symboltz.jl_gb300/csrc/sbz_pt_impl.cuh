@@ -358,6 +358,46 @@ __device__ __forceinline__ void matvec_dtau(const Grp<NW>& g, const double* x, c
   }
 }
 
+// out = J(τ) x and dout = (dJ/dτ) x from one read of x and one evaluation of the metric functionals
+// (the accepted step's f(t1, y1) and the next step's ∂f/∂τ share the t1 coefficient set).
+template <int NW, int NSL>
+__device__ __forceinline__ void matvec_jd(const Grp<NW>& g, const double* x, const CSet& C, const CompDesc* __restrict__ comps,
+                                          const ModelDesc& M, double k, double (&out)[NSL], double (&dout)[NSL]) {
+  const int gt = g.gt;
+  double psi = 0, dpsi = 0, phd = 0, dphd = 0;
+  const double* cv = C.cv; const double* cvd = C.cvd;
+  if (g.pp) {  // warp-uniform, as in matvec
+    double rho, drho;
+    functionals(g.fc, x, C.w, psi, rho);
+    functionals(g.fc, x, C.wd, dpsi, drho);
+    phd = phidot(cv, rho, x[0], psi);
+    dphd = cvd[CV_PA] * rho + cv[CV_PA] * drho + cvd[CV_PB] * x[0] + cvd[CV_MH] * psi + cv[CV_MH] * dpsi;
+  }
+  const double k34 = 0.75 * k;
+#pragma unroll
+  for (int s = 0; s < NSL; ++s) {
+    const int i = comp_of<NW>(gt, s);
+    double o = 0, d = 0;
+    if (i < M.n) {
+      const CompDesc& D = comps[i];
+      const double ax = D.A * x[D.ip] + D.C * x[D.inx], xi = x[i];
+      o = cv[D.sp] * ax + (cv[D.dg] + cv[D.tr]) * xi;
+      d = cvd[D.sp] * ax + (cvd[D.dg] + cvd[D.tr]) * xi;
+      if (s == 0 && gt < 32) {
+        const double x0 = x[D.e0c], x1 = x[D.e1c], x2 = x[D.e2c], xd = x[D.dxa] - k34 * x[D.dxb];
+        o += cv[D.e0] * x0 + cv[D.e1] * x1 + cv[D.e2] * x2 + cv[D.dx] * xd;
+        d += cvd[D.e0] * x0 + cvd[D.e1] * x1 + cvd[D.e2] * x2 + cvd[D.dx] * xd;
+      }
+      if ((g.pp >> s) & 1u) {
+        o += cv[D.phid] * phd + cv[D.psid] * psi;
+        d += cvd[D.phid] * phd + cv[D.phid] * dphd + cvd[D.psid] * psi + cv[D.psid] * dpsi;
+      }
+    }
+    out[s] = o;
+    dout[s] = d;
+  }
+}
+
 // ------------------------------------------------------------------------------------------
 // structured factorisation of M = s I - B and its solves
 //
@@ -960,7 +1000,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
 #pragma unroll
       for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl]; }
       g.sync();
-      matvec<NW, NSL>(g, W.x, W.cs[sJ], comps, M, k, f0);
+      matvec_jd<NW, NSL>(g, W.x, W.cs[sJ], comps, M, k, f0, ft);  // f(t, y) and ∂f/∂τ
       // initial step (Hairer-Nørsett-Wanner II.4)
       double h;
       {
@@ -993,7 +1033,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
       }
       constexpr double kLogErrFloor = -9.210340371976184;  // log(1e-4): the controller's floor on errold
       double lerrold = kLogErrFloor;  // log of the previous accepted error norm
-      bool rejected = false, nonfinite = false, have_jac = false;
+      bool rejected = false, nonfinite = false;
       Factor<ST> F;
       int64_t iters = 0;
       while (t < tend) {
@@ -1001,14 +1041,6 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         if (t + 1.01 * h >= tend) h = tend - t;
         if (!(h > 1e-14 * t)) { status = nonfinite ? SBZ_NONFINITE : SBZ_DTMIN; break; }
         const CSet& CJ = W.cs[sJ];
-        if (!have_jac) {
-          // ∂f/∂τ at the step start (J's coefficients are the previous step-end set)
-#pragma unroll
-          for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y[sl]; }
-          g.sync();
-          matvec_dtau<NW, NSL>(g, W.x, CJ, comps, M, k, ft);
-          have_jac = true;
-        }
         const double ih = 1.0 / h, s = 1.0 / (h * TB::gam);
         const double tn = (h == tend - t) ? tend : t + h;
         // coefficient set of each later stage time: 1..NTIME-1 in place, the step end in sE
@@ -1095,9 +1127,10 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
 #pragma unroll
           for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y1[sl]; }
           g.sync();
+          // f(t1, y1) and the next step's ∂f/∂τ = (dJ/dτ)(t1) y1, both from the t1 coefficient set,
+          // which becomes the next step's Jacobian set
           double f1[NSL];
-          matvec<NW, NSL>(g, W.x, W.cs[sE], comps, M, k, f1);
-          // the t1 coefficient set becomes the next step's Jacobian set
+          matvec_jd<NW, NSL>(g, W.x, W.cs[sE], comps, M, k, f1, ft);
           { const int tsw = sJ; sJ = sE; sE = tsw; }
           if (taus && jout < A.ntau && taus[jout] <= tn) {
             // continuous extension y(t + θh) = (1-θ) y + θ (y1 + (1-θ)(K0 + θ K1 + θ² K2))
@@ -1136,7 +1169,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
             lerrold = fmax(lerr, kLogErrFloor);
             h *= fac;
           }
-          rejected = false; nonfinite = false; have_jac = false;
+          rejected = false; nonfinite = false;
           g.sync();  // x readers are done before the next step writes it
         } else {
           ++nrej;
