@@ -22,7 +22,11 @@ constexpr int kNCV = 48;        // coefficient slots
 constexpr int kMaxFun = 16;     // functional terms (Ψ and δρ sums)
 constexpr int kMaxExpr = 80;    // coefficient expressions
 constexpr int kMaxChains = 12;
-constexpr int kNodeStride = 16; // doubles per table node: τ, 1/(τ_{g+1}-τ_g), 14 values
+// doubles per table node: τ_g, 1/(τ_{g+1}-τ_g), the 14 (value, d/dτ) values, then from kNodePow the
+// power-form coefficients a0..a3 of the cubic Hermite interpolant of each of the 7 quantities on
+// [τ_g, τ_{g+1}] in s = (τ - τ_g)/(τ_{g+1} - τ_g) (zero on the last node)
+constexpr int kNodeStride = 44;
+constexpr int kNodePow = 16;
 
 // coefficient slots
 enum : int {

@@ -73,6 +73,7 @@ struct ModeMem {
   double B[kMaxT][B_COUNT], dB[kMaxT][B_COUNT];
   double src[4];      // e^{-κ}, κ̈, κ⃛ at an output time
   double red[2][NW];  // ping-pong group reductions
+  double ctl[4 + kMaxT];  // step control from the controller warp: h, 1/h, 1/(hγ), step end, stage times
   CosmoDesc cdesc;    // the current mode's cosmology (coefficient expressions, bin momenta)
   int item;
 };
@@ -176,84 +177,102 @@ struct ModeK {  // per-mode constants
 };
 
 // ------------------------------------------------------------------------------------------
-// Cubic Hermite interpolation of table quantity c at τ (value, and τ-derivative if want_d).  The node
-// index comes from an FP32 logarithm and can be one off next to a node: every load of the guessed
-// interval is issued at once and repeated only in that rare case.
-__device__ __forceinline__ void table_hermite(const CosmoDesc* __restrict__ cd, const double* __restrict__ tab, double tau, int c,
-                                              bool want_d, double& val, double& der) {
+// Cubic Hermite interpolation of table quantity c at τ (value, and τ-derivative if want_d) from the
+// interval's power-form coefficients (Horner: three FMAs for the value).  The node index comes from
+// an FP32 logarithm and can be one off next to a node: every load of the guessed interval is issued
+// at once and repeated only in that rare case.
+__device__ __forceinline__ void table_cubic(const CosmoDesc* __restrict__ cd, const double* __restrict__ tab, double tau, int c,
+                                            bool want_d, double& val, double& der) {
   const int ntab = cd->ntab;
   int gi = (int)((__logf((float)tau) - (float)cd->lnt0) * (float)cd->idlnt);
   gi = max(0, min(gi, ntab - 2));
   const double* nd = tab + (size_t)gi * kNodeStride;
   double t0 = nd[0], t1 = nd[kNodeStride], ih = nd[1];
-  double v0 = nd[2 + 2 * c], d0 = nd[3 + 2 * c], v1 = nd[kNodeStride + 2 + 2 * c], d1 = nd[kNodeStride + 3 + 2 * c];
+  double a0 = nd[kNodePow + 4 * c], a1 = nd[kNodePow + 4 * c + 1], a2 = nd[kNodePow + 4 * c + 2], a3 = nd[kNodePow + 4 * c + 3];
   const int shift = (tau < t0 && gi > 0) ? -1 : (tau > t1 && gi < ntab - 2) ? 1 : 0;
   if (shift) {
     nd += shift * kNodeStride;
-    t0 = nd[0]; t1 = nd[kNodeStride]; ih = nd[1];
-    v0 = nd[2 + 2 * c]; d0 = nd[3 + 2 * c]; v1 = nd[kNodeStride + 2 + 2 * c]; d1 = nd[kNodeStride + 3 + 2 * c];
+    t0 = nd[0]; ih = nd[1];
+    a0 = nd[kNodePow + 4 * c]; a1 = nd[kNodePow + 4 * c + 1]; a2 = nd[kNodePow + 4 * c + 2]; a3 = nd[kNodePow + 4 * c + 3];
   }
-  const double h = t1 - t0;
-  const double s = (tau - t0) * ih, s2 = s * s, s3 = s2 * s;
-  val = (2 * s3 - 3 * s2 + 1) * v0 + (s3 - 2 * s2 + s) * h * d0 + (3 * s2 - 2 * s3) * v1 + (s3 - s2) * h * d1;
-  der = want_d ? ((6 * s2 - 6 * s) * v0 + (6 * s - 6 * s2) * v1) * ih + (3 * s2 - 4 * s + 1) * d0 + (3 * s2 - 2 * s) * d1 : 0.0;
+  const double s = (tau - t0) * ih;
+  val = fma(s, fma(s, fma(s, a3, a2), a1), a0);
+  der = want_d ? fma(s, fma(s, 3.0 * a3, 2.0 * a2), a1) * ih : 0.0;
 }
 
 // ------------------------------------------------------------------------------------------
 // τ-dependent coefficients at nt ≤ kMaxT times into sets cs[set[q]]; derivative sets where bit q
 // of dmask is set.  source = true (nt = 1): also fetch e^{-κ}, κ̈, κ⃛ and use the Taylor-mode κ̈
 // as dκ̇/dτ (the line-of-sight sources differentiate the background along its ODE,
-// src/models/cosmologies.jl:99-105).  Warp p forms the base scalars of times 4p..4p+3, lane =
-// 8 (q - 4p) + c: lane c < 7 interpolates table quantity c at time q once; lanes c = 0, 1, 7 then share one
-// reciprocal path (1/a, 1/ℋ, 1/τ) and lanes c < nx one momentum-bin energy path (a from lane 8q by
-// shuffle), so no quantity is interpolated twice.  The expressions are then spread over the group.
-// The caller guarantees that no thread still reads the target sets; the call ends with a group
-// barrier.
+// src/models/cosmologies.jl:99-105).  Warp p forms the base scalars of times 2p, 2p+1, lane =
+// 16 (q - 2p) + c: lane c < 7 interpolates table quantity c at time q once; then every lane of the
+// time takes one reciprocal square root, so the FP64 work is one instruction stream for all of
+// them: lane 8 + j the energy of momentum bin j, E_j = sqrt(x_j² + (y0 a)²), lanes 5, 6, 7 the
+// reciprocals 1/a, 1/ℋ, 1/τ as rsqrt(v²) (v > 0), with dr/dτ = -u r³, u = (1/2) dw/dτ for the
+// derivative sets.  The expressions are then spread over the group.  The caller guarantees that no
+// thread still reads the target sets; the call ends with a group barrier.
 template <int NW, int NSL, typename ST>
 __device__ __forceinline__ void coef_eval(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const int* set, const double* taus, int nt,
                           unsigned dmask, bool source, const CosmoDesc* cd, const double* __restrict__ tab,
                           int nexpr, int nx, const ModeK& mk) {
-  // times 4p..4p+3 in pass p: warp p of the group, or every pass on the one warp when NW = 1
-  for (int pass = NW == 1 ? 0 : g.wq; 4 * pass < nt; pass += NW) {
-    const int lane = g.lane, q = 4 * pass + (lane >> 3), c = lane & 7;
+  // times 2p, 2p+1 in pass p: warp p of the group, or every pass on the one warp when NW = 1
+  for (int pass = NW == 1 ? 0 : g.wq; 2 * pass < nt; pass += NW) {
+    const int lane = g.lane, q = 2 * pass + (lane >> 4), c = lane & 15;
     const bool live = q < nt;
     const bool dq = live && ((dmask >> q) & 1u);
     double v = 0, d = 0;
-    if (live && c < 7) table_hermite(cd, tab, taus[q], c, dq, v, d);
-    const double a = __shfl_sync(FULL, v, lane & ~7), da = __shfl_sync(FULL, d, lane & ~7);
+    if (live && c < 7) table_cubic(cd, tab, taus[q], c, dq, v, d);
+    const int base = lane & ~15;
+    const double a = __shfl_sync(FULL, v, base), da = __shfl_sync(FULL, d, base);
+    const double hc = __shfl_sync(FULL, v, base + 1), dhc = __shfl_sync(FULL, d, base + 1);
+    const double tq = live ? taus[q] : 1.0;
     double* Bq = W.B[live ? q : 0]; double* dBq = W.dB[live ? q : 0];
-    if (live && (c <= 1 || c == 7)) {  // reciprocals of a, ℋ, τ
-      const double rv = c == 7 ? taus[q] : v, drv = c == 7 ? 1.0 : d;
-      const double inv = 1.0 / rv;
-      if (c == 0) {
-        Bq[B_IA] = inv; Bq[B_IA2] = inv * inv; Bq[B_R] = cd->R0 * inv;
-        if (dq) { const double dia = -drv * inv * inv; dBq[B_IA] = dia; dBq[B_IA2] = 2 * inv * dia; dBq[B_R] = cd->R0 * dia; }
-      } else if (c == 1) {
-        Bq[B_H] = v; Bq[B_IH] = inv;
-        if (dq) { dBq[B_H] = d; dBq[B_IH] = -drv * inv * inv; }
-      } else {
-        Bq[B_ITAU] = inv; Bq[B_ONE] = 1; Bq[B_K] = mk.k; Bq[B_K2] = mk.k2; Bq[B_IK] = mk.ik; Bq[B_IK2] = mk.ik2;
-        if (dq) { dBq[B_ITAU] = -inv * inv; dBq[B_ONE] = 0; dBq[B_K] = 0; dBq[B_K2] = 0; dBq[B_IK] = 0; dBq[B_IK2] = 0; }
-      }
-    } else if (live && c == 2) {  // κ̇ (for the sources, dκ̇/dτ is κ̈ from lane c = 5)
-      Bq[B_KD] = v;
-      if (dq && !source) dBq[B_KD] = d;
-    } else if (live && c == 3) {  // c_s²
-      Bq[B_CS2] = v;
-      if (dq) dBq[B_CS2] = d;
-    } else if (live && c < 7 && source) {  // e^{-κ}, κ̈, κ⃛
-      W.src[c - 4] = v;
-      if (c == 5) dBq[B_KD] = v;
+    const int j = c - 8;
+    const bool bin = j >= 0 && j < nx;
+    const double xj = bin ? cd->xq[j] : 0.0, ixj = bin ? cd->ixq[j] : 0.0;
+    const double x = bin ? xj : c == 5 ? a : c == 6 ? hc : c == 7 ? tq : 1.0;
+    const double dx = bin ? 0.0 : c == 5 ? da : c == 6 ? dhc : 1.0;
+    const double ys = bin ? cd->y0 : 0.0;
+    const double ya = ys * a;
+    const double w = fma(x, x, ya * ya);
+    const double r = rsqrt(w);
+    const double E = w * r;
+    const double p2 = (bin ? xj : r) * r;                     // bins: x_j / E; lane 5: 1/a²
+    const double p3 = (bin ? E : cd->R0) * (bin ? ixj : r);  // bins: E / x_j; lane 5: R0 / a
+    double ur = 0, dr = 0, dp2 = 0, dp3 = 0;
+    if (dq) {
+      const double u = fma(x, dx, ya * (ys * da));
+      ur = u * r;                                   // bins: dE/dτ
+      dr = -ur * (r * r);
+      dp2 = (bin ? xj : r) * dr;                    // bins: d(x_j/E)/dτ; lane 5: half of d(1/a²)/dτ
+      dp3 = (bin ? ur : cd->R0) * (bin ? ixj : dr);
     }
-    if (live && c < nx) {  // momentum-bin energy E_c = sqrt(x_c² + (y0 a)²)
-      const double xj = cd->xq[c], y0a = cd->y0 * a;
-      const double E2 = xj * xj + y0a * y0a;
-      const double iE = rsqrt(E2), E = E2 * iE;
-      const double ixj = cd->ixq[c];
-      Bq[B_Q + c] = xj * iE; Bq[B_IQ + c] = E * ixj; Bq[B_E + c] = E; Bq[B_IE + c] = iE;
-      if (dq) {
-        const double dE = cd->y0 * y0a * da * iE;
-        dBq[B_Q + c] = -xj * dE * iE * iE; dBq[B_IQ + c] = dE * ixj; dBq[B_E + c] = dE; dBq[B_IE + c] = -dE * iE * iE;
+    if (live) {
+      if (bin) {
+        Bq[B_Q + j] = p2; Bq[B_IQ + j] = p3; Bq[B_E + j] = E; Bq[B_IE + j] = r;
+        if (dq) { dBq[B_Q + j] = dp2; dBq[B_IQ + j] = dp3; dBq[B_E + j] = ur; dBq[B_IE + j] = dr; }
+      } else if (c == 5) {
+        Bq[B_IA] = r; Bq[B_IA2] = p2; Bq[B_R] = p3;
+        if (dq) { dBq[B_IA] = dr; dBq[B_IA2] = 2.0 * dp2; dBq[B_R] = dp3; }
+      } else if (c == 6) {
+        Bq[B_IH] = r;
+        if (dq) dBq[B_IH] = dr;
+      } else if (c == 7) {
+        Bq[B_ITAU] = r; Bq[B_ONE] = 1; Bq[B_K] = mk.k; Bq[B_K2] = mk.k2; Bq[B_IK] = mk.ik; Bq[B_IK2] = mk.ik2;
+        if (dq) { dBq[B_ITAU] = dr; dBq[B_ONE] = 0; dBq[B_K] = 0; dBq[B_K2] = 0; dBq[B_IK] = 0; dBq[B_IK2] = 0; }
+      }
+      if (c == 1) {  // ℋ
+        Bq[B_H] = v;
+        if (dq) dBq[B_H] = d;
+      } else if (c == 2) {  // κ̇ (for the sources, dκ̇/dτ is κ̈ from lane c = 5)
+        Bq[B_KD] = v;
+        if (dq && !source) dBq[B_KD] = d;
+      } else if (c == 3) {  // c_s²
+        Bq[B_CS2] = v;
+        if (dq) dBq[B_CS2] = d;
+      } else if (c >= 4 && c < 7 && source) {  // e^{-κ}, κ̈, κ⃛
+        W.src[c - 4] = v;
+        if (c == 5) dBq[B_KD] = v;
       }
     }
   }
@@ -684,39 +703,38 @@ __device__ __forceinline__ void factorize(const Grp<NW>& g, ModeMem<NW, NSL, ST>
       }
     }
   }
-  if (g.wq == 0) {  // head inverse: Gauss-Jordan with partial pivoting, lane r holds row r
-    const int r = lane;
-    ST a[8], e[8];
+  if (g.wq == 0) {
+    // head inverse: Gauss-Jordan with partial pivoting on [H | I], lane q (mod 16) holding column q
+    // in registers, so the pivot search is lane kk's own register scan and a pivot step moves only
+    // the pivot row index, the pivot and the eliminated column's multipliers between lanes
+    const int q = lane & 15;
+    ST col[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) { a[q] = r < 8 ? W.H[r * 8 + q] : ST(0); e[q] = (q == r) ? ST(1) : ST(0); }
-    if (r == 4) a[4] -= W.hcorr[0];  // F2 (Schur complement of the F tail)
-    if (r == 7) a[7] -= W.hcorr[1];  // G2 (G tail)
+    for (int r = 0; r < 8; ++r) col[r] = q < 8 ? W.H[r * 8 + q] : ST(r == q - 8 ? 1 : 0);
+    if (q == 4) col[4] -= W.hcorr[0];  // F2 (Schur complement of the F tail)
+    if (q == 7) col[7] -= W.hcorr[1];  // G2 (G tail)
 #pragma unroll
     for (int kk = 0; kk < 8; ++kk) {
-      ST val = (r >= kk && r < 8) ? fabs(a[kk]) : ST(-1);
-      int idx = r;
+      int p = kk;  // first row of largest magnitude at or below kk (meaningful on lane kk)
+      ST best = fabs(col[kk]);
 #pragma unroll
-      for (int o = 1; o < 8; o <<= 1) {
-        const ST ov = __shfl_xor_sync(FULL, val, o);
-        const int oi = __shfl_xor_sync(FULL, idx, o);
-        if (ov > val || (ov == val && oi < idx)) { val = ov; idx = oi; }
-      }
-      const int p = __shfl_sync(FULL, idx, 0);
-      const int src = r == kk ? p : r == p ? kk : r;
+      for (int r = kk + 1; r < 8; ++r) { const ST v = fabs(col[r]); if (v > best) { best = v; p = r; } }
+      p = __shfl_sync(FULL, p, kk);
+      ST vp = col[kk];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) { a[q] = __shfl_sync(FULL, a[q], src); e[q] = __shfl_sync(FULL, e[q], src); }
-      const ST ip = rcp<ST>(__shfl_sync(FULL, a[kk], kk));
-      const ST fct = a[kk];
+      for (int r = kk + 1; r < 8; ++r) if (r == p) { vp = col[r]; col[r] = col[kk]; }
+      col[kk] = vp;
+      ST m[8];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const ST pa = __shfl_sync(FULL, a[q], kk) * ip, pe = __shfl_sync(FULL, e[q], kk) * ip;
-        if (r == kk) { a[q] = pa; e[q] = pe; }
-        else { a[q] -= fct * pa; e[q] -= fct * pe; }
-      }
+      for (int r = 0; r < 8; ++r) m[r] = __shfl_sync(FULL, col[r], kk);  // column kk after the swap
+      const ST ip = rcp<ST>(m[kk]);
+      col[kk] *= ip;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) if (r != kk) col[r] -= m[r] * col[kk];
     }
-    if (r < 8) {
+    if (lane >= 8 && lane < 16) {
 #pragma unroll
-      for (int q = 0; q < 8; ++q) W.Hinv[r * 8 + q] = e[q];
+      for (int r = 0; r < 8; ++r) W.Hinv[r * 8 + (lane - 8)] = col[r];
     }
   }
   F.is = (ST)(h * gam);
@@ -1032,38 +1050,46 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         if (!isfinite(h) || h <= 0) h = 1e-6 * fmax(1.0, t);
       }
       constexpr double kLogErrFloor = -9.210340371976184;  // log(1e-4): the controller's floor on errold
-      double lerrold = kLogErrFloor;  // log of the previous accepted error norm
+      double lerrold = kLogErrFloor;  // log of the previous accepted error norm (controller warp)
       bool rejected = false, nonfinite = false;
       Factor<ST> F;
       int64_t iters = 0;
-      while (t < tend) {
-        if (++iters > A.maxiters) { status = SBZ_MAXITERS; break; }
-        if (t + 1.01 * h >= tend) h = tend - t;
-        if (!(h > 1e-14 * t)) { status = nonfinite ? SBZ_NONFINITE : SBZ_DTMIN; break; }
-        const CSet& CJ = W.cs[sJ];
-        const double ih = 1.0 / h, s = 1.0 / (h * TB::gam);
-        const double tn = (h == tend - t) ? tend : t + h;
-        // coefficient set of each later stage time: 1..NTIME-1 in place, the step end in sE
-        int tset[TB::NTIME + 1];
-#pragma unroll
-        for (int q = 1; q < TB::NTIME; ++q) tset[q] = q;
-        tset[TB::NTIME] = sE;
-        {
-          // coefficients at the later stage times (the last one, t + h, with τ-derivatives: it is
-          // the next step's Jacobian set), and the factorisation for this h
-          double tt[TB::NTIME];
+      // Step control runs on one warp (warp 1: no metric functionals in its operator products) while
+      // the others finish the step; the loop-top barrier publishes it: the proposed size clamped to
+      // the end point, 1/h, 1/(hγ), the step end and the stage times (FP64; every warp reads them).
+      const int cw = NW > 1 ? 1 : 0;
+      auto publish = [&](double hp, double tc) {
+        if (tc + 1.01 * hp >= tend) hp = tend - tc;
+        const double te = (hp == tend - tc) ? tend : tc + hp;
+        if (g.lane == 0) {
+          W.ctl[0] = hp; W.ctl[1] = 1.0 / hp; W.ctl[2] = 1.0 / (hp * TB::gam); W.ctl[3] = te;
 #pragma unroll
           for (int q = 1; q < TB::NTIME; ++q) {
             int st = 1;
 #pragma unroll
             for (int i = 1; i < TB::S; ++i) if (TB::tslot(i) == q) st = i;
-            tt[q - 1] = t + TB::c(st) * h;
+            W.ctl[4 + q - 1] = tc + TB::c(st) * hp;
           }
-          tt[TB::NTIME - 1] = tn;
-          g.sync();  // the previous step's readers of these sets are done
-          coef_eval(g, W, tset + 1, tt, TB::NTIME, 1u << (TB::NTIME - 1), false, cd, tab, M.nexpr, M.nx, mk);
-          factorize(g, W, F, CJ, comps, M, k, h, s, TB::gam, scan);
+          W.ctl[4 + TB::NTIME - 1] = te;
         }
+      };
+      if (g.wq == cw) publish(h, t);
+      while (t < tend) {
+        g.sync();  // step control published; the previous step's readers of x and the coefficient sets are done
+        if (++iters > A.maxiters) { status = SBZ_MAXITERS; break; }
+        h = W.ctl[0];
+        if (!(h > 1e-14 * t)) { status = nonfinite ? SBZ_NONFINITE : SBZ_DTMIN; break; }
+        const CSet& CJ = W.cs[sJ];
+        const double ih = W.ctl[1], s = W.ctl[2], tn = W.ctl[3];
+        // coefficient set of each later stage time: 1..NTIME-1 in place, the step end in sE
+        int tset[TB::NTIME + 1];
+#pragma unroll
+        for (int q = 1; q < TB::NTIME; ++q) tset[q] = q;
+        tset[TB::NTIME] = sE;
+        // coefficients at the later stage times (the last one, t + h, with τ-derivatives: it is the
+        // next step's Jacobian set), and the factorisation for this h
+        coef_eval(g, W, tset + 1, W.ctl + 4, TB::NTIME, 1u << (TB::NTIME - 1), false, cd, tab, M.nexpr, M.nx, mk);
+        factorize(g, W, F, CJ, comps, M, k, h, s, TB::gam, scan);
         double U[TB::S][NSL], b[NSL], Fv[NSL], Y[NSL];
         float isk[NSL];  // refinement stopping weights
 #pragma unroll
@@ -1127,6 +1153,16 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
 #pragma unroll
           for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y1[sl]; }
           g.sync();
+          if (g.wq == cw) {
+            // PI controller fac = 0.9 err^-beta1 errold^beta2 (OrdinaryDiffEq's defaults for the
+            // method's order), FP64 in both precisions; log(errold) is kept from the previous acceptance
+            const double lerr = 0.5 * log(fmax(err2, 1e-20));
+            double fac = 0.9 * exp(-TB::beta1 * lerr + TB::beta2 * lerrold);
+            fac = fmin(10.0, fmax(0.2, fac));
+            if (rejected) fac = fmin(fac, 1.0);
+            lerrold = fmax(lerr, kLogErrFloor);
+            publish(h * fac, tn);
+          }
           // f(t1, y1) and the next step's ∂f/∂τ = (dJ/dτ)(t1) y1, both from the t1 coefficient set,
           // which becomes the next step's Jacobian set
           double f1[NSL];
@@ -1159,23 +1195,12 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
 #pragma unroll
           for (int sl = 0; sl < NSL; ++sl) { y[sl] = y1[sl]; f0[sl] = f1[sl]; }
           ++nacc;
-          // PI controller fac = 0.9 err^-beta1 errold^beta2 (OrdinaryDiffEq's defaults for the
-          // method's order), FP64 in both precisions; log(errold) is kept from the previous acceptance
-          {
-            const double lerr = 0.5 * log(fmax(err2, 1e-20));
-            double fac = 0.9 * exp(-TB::beta1 * lerr + TB::beta2 * lerrold);
-            fac = fmin(10.0, fmax(0.2, fac));
-            if (rejected) fac = fmin(fac, 1.0);
-            lerrold = fmax(lerr, kLogErrFloor);
-            h *= fac;
-          }
           rejected = false; nonfinite = false;
-          g.sync();  // x readers are done before the next step writes it
         } else {
           ++nrej;
           rejected = true;
-          if (!isfinite(err2)) { nonfinite = true; h *= 0.2; }
-          else h *= fmax(0.2, 0.9 * exp(-0.5 * TB::rej * log(err2)));
+          if (!isfinite(err2)) nonfinite = true;
+          if (g.wq == cw) publish(nonfinite ? 0.2 * h : h * fmax(0.2, 0.9 * exp(-0.5 * TB::rej * log(err2))), t);
           // J's coefficients (at t) and ∂f/∂τ stay valid; only the factorisation changes
         }
       }
