@@ -297,7 +297,7 @@ static int upload_tables(sbz_problem* pb) {
     if (pb->bg_status[c] != SBZ_OK) {
       sbz::CosmoDesc& D = pb->cds[c];
       std::memset(&D, 0, sizeof D);
-      D.tau_start = D.tau0 = NAN; D.ntab = ntab; D.idlnt = 1;
+      D.tau_start = D.tau0 = NAN; D.ntab = ntab; D.idlnt = 1; D.idlntf = 1;
       continue;
     }
     cos[c] = B.P; kap[c] = B.kappa0; ok[c] = 1;

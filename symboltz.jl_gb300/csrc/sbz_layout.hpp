@@ -80,7 +80,9 @@ struct ModelDesc {
 struct CosmoDesc {
   double tau_start, tau0, taurec;
   double lnt0, idlnt;
-  int ntab, pad;
+  int ntab;
+  float lnt0f, idlntf;  // FP32 copies for the table-node guess
+  int pad;
   double Oc0, Ob0, Og0, On0, wh, y0, R0, As, ns, kpivot;
   double xq[kMaxNx], Wq[kMaxNx], dlnf[kMaxNx], ixq[kMaxNx];
   CoefExpr expr[kMaxExpr];

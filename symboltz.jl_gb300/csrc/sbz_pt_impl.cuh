@@ -58,7 +58,6 @@ struct ModeMem {
   double x[NM + 1];   // operator input; x[n..NM] stay 0
   double f[NM + 1];
   ST r[NM + 1];       // structured-solve right-hand side / work vector
-  ST u[NM];           // W⁻¹ r result
   ST dinv[NM], sub[NM], sup[NM], mfw[NM], dd[NM];
   ST fA[5][NM], bA[5][NM], bP[NM];   // warp-scan multipliers of the chain eliminations, per row
   ST cf[2][kMaxChains];              // forward-eliminated first row of each chain, per vector
@@ -73,7 +72,9 @@ struct ModeMem {
   double B[kMaxT][B_COUNT], dB[kMaxT][B_COUNT];
   double src[4];      // e^{-κ}, κ̈, κ⃛ at an output time
   double red[2][NW];  // ping-pong group reductions
+  float redf[2][NW];
   double ctl[4 + kMaxT];  // step control from the controller warp: h, 1/h, 1/(hγ), step end, stage times
+  int ctlf;               // and its flags
   CosmoDesc cdesc;    // the current mode's cosmology (coefficient expressions, bin momenta)
   int item;
 };
@@ -151,15 +152,50 @@ __device__ __forceinline__ float group_max(const Grp<NW>& g, ModeMem<NW, NSL, ST
     __syncwarp();
     return v;
   } else {
-    if (g.lane == 0) W.red[g.rp][g.wq] = v;
+    if (g.lane == 0) W.redf[g.rp][g.wq] = v;
     g.sync();
     float s = 0;
 #pragma unroll
-    for (int w = 0; w < NW; ++w) s = fmaxf(s, (float)W.red[g.rp][w]);
+    for (int w = 0; w < NW; ++w) s = fmaxf(s, W.redf[g.rp][w]);
     g.rp ^= 1;
     return s;
   }
 }
+
+// FP32 <-> FP64 conversions with integer operations.  The FP64 pipe of this GPU issues one warp
+// instruction per 64 cycles, conversions and comparisons included, while these are a handful of
+// integer-pipe instructions.  Both are exact for normal numbers and zero (FP64 -> FP32 rounds to
+// nearest even, as the hardware conversion does); FP32 subnormals are flushed to zero, results
+// beyond the FP32 range become ±inf, NaN stays NaN.
+__device__ __forceinline__ double f32_to_f64(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu, sg = u & 0x80000000u;
+  const unsigned de = e == 0xffu ? 0x7ffu : e + 896u;
+  const unsigned hi = e == 0 ? sg : (sg | (de << 20) | ((u & 0x7fffffu) >> 3));
+  const unsigned lo = e == 0 ? 0u : (u << 29);
+  return __hiloint2double((int)hi, (int)lo);
+}
+__device__ __forceinline__ float f64_to_f32(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const unsigned sg = hi & 0x80000000u, ex = (hi >> 20) & 0x7ffu;
+  const int e = (int)ex - 896;
+  const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29), rest = lo & 0x1fffffffu;
+  unsigned r = ((unsigned)e << 23) + m;
+  r += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;  // a carry moves into the exponent
+  r = e <= 0 ? 0u : (e >= 255 ? 0x7f800000u : r);
+  if (ex == 0x7ffu) r = ((hi & 0xfffffu) | lo) ? 0x7fc00000u : 0x7f800000u;
+  return __uint_as_float(sg | r);
+}
+template <typename ST>
+__device__ __forceinline__ ST to_st(double v);
+template <>
+__device__ __forceinline__ float to_st<float>(double v) { return f64_to_f32(v); }
+template <>
+__device__ __forceinline__ double to_st<double>(double v) { return v; }
+__device__ __forceinline__ double from_st(float v) { return f32_to_f64(v); }
+__device__ __forceinline__ double from_st(double v) { return v; }
+// Order of non-negative doubles (and NaN above +inf) by their bit patterns: integer comparisons.
+__device__ __forceinline__ long long dkey(double v) { return __double_as_longlong(v); }
 
 template <typename ST>
 __device__ __forceinline__ ST rcp(ST v);
@@ -184,12 +220,13 @@ struct ModeK {  // per-mode constants
 __device__ __forceinline__ void table_cubic(const CosmoDesc* __restrict__ cd, const double* __restrict__ tab, double tau, int c,
                                             bool want_d, double& val, double& der) {
   const int ntab = cd->ntab;
-  int gi = (int)((__logf((float)tau) - (float)cd->lnt0) * (float)cd->idlnt);
+  int gi = (int)((__logf(f64_to_f32(tau)) - cd->lnt0f) * cd->idlntf);
   gi = max(0, min(gi, ntab - 2));
   const double* nd = tab + (size_t)gi * kNodeStride;
   double t0 = nd[0], t1 = nd[kNodeStride], ih = nd[1];
   double a0 = nd[kNodePow + 4 * c], a1 = nd[kNodePow + 4 * c + 1], a2 = nd[kNodePow + 4 * c + 2], a3 = nd[kNodePow + 4 * c + 3];
-  const int shift = (tau < t0 && gi > 0) ? -1 : (tau > t1 && gi < ntab - 2) ? 1 : 0;
+  const long long kt = dkey(tau);  // τ and the node times are positive
+  const int shift = (kt < dkey(t0) && gi > 0) ? -1 : (kt > dkey(t1) && gi < ntab - 2) ? 1 : 0;
   if (shift) {
     nd += shift * kNodeStride;
     t0 = nd[0]; ih = nd[1];
@@ -277,24 +314,52 @@ __device__ __forceinline__ void coef_eval(const Grp<NW>& g, ModeMem<NW, NSL, ST>
     }
   }
   g.sync();
-  for (int p = g.gt; p < nt * nexpr; p += 32 * NW) {
-    const int q = p / nexpr, e = p - q * nexpr;
+  // expression e at time q (with its τ-derivative when deriv): K1 p0 p1 p2 + K2 q0 q1 q2
+  auto expr = [&](int q, int e, bool deriv) {
     const CoefExpr& X = cd->expr[e];
     const double* Bq = W.B[q];
     const double p0 = Bq[X.b[0]], p1 = Bq[X.b[1]], p2 = Bq[X.b[2]];
     const double q0 = Bq[X.b[3]], q1 = Bq[X.b[4]], q2 = Bq[X.b[5]];
-    const double val = X.K1 * (p0 * p1 * p2) + X.K2 * (q0 * q1 * q2);
+    const double p12 = p1 * p2, q12 = q1 * q2;
+    const double val = fma(X.K1, p0 * p12, X.K2 * (q0 * q12));
     double dval = 0;
-    if ((dmask >> q) & 1u) {
+    if (deriv) {
       const double* dBq = W.dB[q];
       const double dp0 = dBq[X.b[0]], dp1 = dBq[X.b[1]], dp2 = dBq[X.b[2]];
       const double dq0 = dBq[X.b[3]], dq1 = dBq[X.b[4]], dq2 = dBq[X.b[5]];
-      dval = X.K1 * (dp0 * p1 * p2 + p0 * dp1 * p2 + p0 * p1 * dp2) + X.K2 * (dq0 * q1 * q2 + q0 * dq1 * q2 + q0 * q1 * dq2);
+      const double dP = fma(dp0, p12, p0 * fma(dp1, p2, p1 * dp2));
+      const double dQ = fma(dq0, q12, q0 * fma(dq1, q2, q1 * dq2));
+      dval = fma(X.K1, dP, X.K2 * dQ);
     }
     CSet& C = W.cs[set[q]];
     const int d = X.dest;
     if (d < kNCV) { C.cv[d] = val; C.cvd[d] = dval; }
     else { C.w[d - kNCV] = val; C.wd[d - kNCV] = dval; }
+  };
+  // the qi-th time with (deriv) or without derivatives
+  auto time_of = [&](int qi, bool deriv) {
+    int q = 0;
+    for (int qq = 0, cnt = 0; qq < nt; ++qq)
+      if ((((dmask >> qq) & 1u) != 0) == deriv) { if (cnt == qi) q = qq; ++cnt; }
+    return q;
+  };
+  const unsigned dm = dmask & ((1u << nt) - 1u);
+  const int nder = __popc(dm) * nexpr, nval = nt * nexpr - nder;
+  const int wd = (nder + 31) >> 5;  // warps for the derivative expressions, one per lane
+  if (NW >= 4 && wd > 0 && wd < NW) {
+    // derivative expressions (about three times the FP64 work of a value) on the top wd warps, one
+    // per lane; the value-only expressions spread over the other warps
+    if (g.wq >= NW - wd) {
+      const int i = (g.wq - (NW - wd)) * 32 + g.lane;
+      if (i < nder) { const int qi = i / nexpr; expr(time_of(qi, true), i - qi * nexpr, true); }
+    } else {
+      for (int i = g.gt; i < nval; i += 32 * (NW - wd)) { const int qi = i / nexpr; expr(time_of(qi, false), i - qi * nexpr, false); }
+    }
+  } else {
+    for (int p = g.gt; p < nt * nexpr; p += 32 * NW) {
+      const int q = p / nexpr;
+      expr(q, p - q * nexpr, ((dmask >> q) & 1u) != 0);
+    }
   }
   g.sync();
 }
@@ -465,15 +530,21 @@ __device__ __forceinline__ void solve_M(const Grp<NW>& g, ModeMem<NW, NSL, ST>& 
       const ChainPair c = chain_pair(M, p);
       const int i0 = c.l0 - lane, i1 = c.l1 - lane;
       const bool on0 = i0 >= c.f0, on1 = i1 >= c.f1;
+      // every load unconditional from a row inside the arrays (off-chain lanes read row 0), then
+      // zeroed by a select: no branch around the loads
+      const int j0 = on0 ? i0 : 0, j1 = on1 ? i1 : 0;
       ST m0[5], m1[5], n0[5], n1[5];
 #pragma unroll
       for (int q = 0; q < 5; ++q) {
-        m0[q] = on0 ? W.fA[q][i0] : ST(0); m1[q] = on1 ? W.fA[q][i1] : ST(0);
-        n0[q] = on0 ? W.bA[q][i0] : ST(0); n1[q] = on1 ? W.bA[q][i1] : ST(0);
+        const ST a0 = W.fA[q][j0], a1 = W.fA[q][j1], b0 = W.bA[q][j0], b1 = W.bA[q][j1];
+        m0[q] = on0 ? a0 : ST(0); m1[q] = on1 ? a1 : ST(0);
+        n0[q] = on0 ? b0 : ST(0); n1[q] = on1 ? b1 : ST(0);
       }
-      const ST d0 = on0 ? W.dinv[i0] : ST(0), d1 = on1 ? W.dinv[i1] : ST(0);
-      ST x0 = on0 ? v0[i0] : ST(0), x1 = on1 ? v0[i1] : ST(0);
-      ST y0 = (NV > 1 && on0) ? v1[i0] : ST(0), y1 = (NV > 1 && on1) ? v1[i1] : ST(0);
+      const ST e0 = W.dinv[j0], e1 = W.dinv[j1], r0 = v0[j0], r1 = v0[j1];
+      const ST d0 = on0 ? e0 : ST(0), d1 = on1 ? e1 : ST(0);
+      ST x0 = on0 ? r0 : ST(0), x1 = on1 ? r1 : ST(0);
+      ST y0 = ST(0), y1 = ST(0);
+      if (NV > 1) { const ST s0 = v1[j0], s1 = v1[j1]; y0 = on0 ? s0 : ST(0); y1 = on1 ? s1 : ST(0); }
 #pragma unroll
       for (int q = 0; q < 5; ++q) {  // forward elimination, up the lanes
         const int d = 1 << q;
@@ -613,15 +684,15 @@ __device__ __forceinline__ void factorize(const Grp<NW>& g, ModeMem<NW, NSL, ST>
     if (i < M.n) {
       const CompDesc& D = comps[i];
       const double spv = cv[D.sp];
-      W.dd[i] = (ST)(s - (cv[D.dg] + cv[D.tr]));
-      W.sup[i] = (ST)(-spv * D.C);
-      W.sub[i] = (ST)(-spv * D.A);
-      W.Z1[i] = (ST)cv[D.phid];
-      W.Z2[i] = (ST)cv[D.psid];
+      W.dd[i] = to_st<ST>(s - (cv[D.dg] + cv[D.tr]));
+      W.sup[i] = to_st<ST>(-spv * D.C);
+      W.sub[i] = to_st<ST>(-spv * D.A);
+      W.Z1[i] = to_st<ST>(cv[D.phid]);
+      W.Z2[i] = to_st<ST>(cv[D.psid]);
     }
   }
-  for (int q = gt; q < kWF; q += 32 * NW) W.wS[q] = (ST)C.w[q];
-  if (gt < 3) W.fS[gt] = (ST)cv[gt == 0 ? CV_PA : gt == 1 ? CV_PB : CV_MH];
+  for (int q = gt; q < kWF; q += 32 * NW) W.wS[q] = to_st<ST>(C.w[q]);
+  if (gt < 3) W.fS[gt] = to_st<ST>(cv[gt == 0 ? CV_PA : gt == 1 ? CV_PB : CV_MH]);
   g.sync();
   for (int ch = gt; ch < M.nchain; ch += 32 * NW) {  // chain LU from the truncation end (precision ST)
     const int first = M.chFirst[ch], last = M.chLast[ch], at = M.chAttach[ch];
@@ -635,7 +706,7 @@ __device__ __forceinline__ void factorize(const Grp<NW>& g, ModeMem<NW, NSL, ST>
     }
     if (at >= 0) {
       const CompDesc& D = comps[at];
-      const ST hs = (ST)(-cv[D.sp] * D.C);  // coefficient of x[first] in the head row
+      const ST hs = to_st<ST>(-cv[D.sp] * D.C);  // coefficient of x[first] in the head row
       const ST hm = hs * dn;
       W.hmul[ch] = hm;
       W.hcorr[ch] = hm * W.sub[first];
@@ -659,7 +730,7 @@ __device__ __forceinline__ void factorize(const Grp<NW>& g, ModeMem<NW, NSL, ST>
     if ((c = head_local(D.dxa)) >= 0) row[c] -= cv[D.dx];
     if ((c = head_local(D.dxb)) >= 0) row[c] += k34 * cv[D.dx];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) W.H[j * 8 + q] = (ST)row[q];
+    for (int q = 0; q < 8; ++q) W.H[j * 8 + q] = to_st<ST>(row[q]);
   }
   g.sync();
   const int npair = (M.nchain + 1) >> 1;
@@ -737,8 +808,8 @@ __device__ __forceinline__ void factorize(const Grp<NW>& g, ModeMem<NW, NSL, ST>
       for (int r = 0; r < 8; ++r) W.Hinv[r * 8 + (lane - 8)] = col[r];
     }
   }
-  F.is = (ST)(h * gam);
-  F.ihc = rcp<ST>((ST)(s - cv[CV_MH]));
+  F.is = to_st<ST>(h * gam);
+  F.ihc = rcp<ST>(to_st<ST>(s - cv[CV_MH]));
   g.sync();
   // rank-2 correction: Z1 = M⁻¹ c_Φ̇, Z2 = M⁻¹ c_Ψ
   solve_M<2>(g, W, M, F, scan, W.Z1, W.Z2);
@@ -755,11 +826,11 @@ __device__ __forceinline__ void factorize(const Grp<NW>& g, ModeMem<NW, NSL, ST>
   F.S00 = d * idet; F.S01 = -b * idet; F.S10 = -c * idet; F.S11 = a * idet;
 }
 
-// W.u = W⁻¹ W.r for the thread's own components (W.r complete on entry; W.r is overwritten).
-// Only own slots of W.u are written, so no barrier follows.
+// u = W⁻¹ W.r for the thread's own components, in registers (W.r complete on entry; W.r is
+// overwritten; no barrier follows).
 template <int NW, int NSL, typename ST>
 __device__ __forceinline__ void solve_W(const Grp<NW>& g, ModeMem<NW, NSL, ST>& W, const Factor<ST>& F, const ModelDesc& M,
-                                        bool scan) {
+                                        bool scan, ST (&u)[NSL]) {
   solve_M<1>(g, W, M, F, scan, W.r, W.r);
   ST psi, ph;
   functionals_st(g, W, W.r, psi, ph);
@@ -767,11 +838,11 @@ __device__ __forceinline__ void solve_W(const Grp<NW>& g, ModeMem<NW, NSL, ST>& 
 #pragma unroll
   for (int sl = 0; sl < NSL; ++sl) {
     const int i = comp_of<NW>(g.gt, sl);
-    if (i < M.n) {
-      ST ri = W.r[i];
-      if (W.att[i] >= 0) ri += W.bP[i] * W.r[W.att[i]];  // head-value term of the chain back substitution
-      W.u[i] = ri + W.Z1[i] * t0 + W.Z2[i] * t1;
-    }
+    const int ic = i < M.n ? i : 0;
+    const int at = W.att[ic];
+    const ST ri = W.r[ic], ra = W.r[at >= 0 ? at : ic], P = W.bP[ic], z1 = W.Z1[ic], z2 = W.Z2[ic];
+    const ST rh = at >= 0 ? ri + P * ra : ri;  // head-value term of the chain back substitution
+    u[sl] = i < M.n ? rh + z1 * t0 + z2 * t1 : ST(0);
   }
 }
 
@@ -788,11 +859,12 @@ __device__ __forceinline__ void stage_solve(const Grp<NW>& g, ModeMem<NW, NSL, S
                             float* first_correction = nullptr) {
   const int gt = g.gt;
 #pragma unroll
-  for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) W.r[i] = (ST)b[sl]; }
+  for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) W.r[i] = to_st<ST>(b[sl]); }
   g.sync();
-  solve_W(g, W, F, M, scan);
+  ST u[NSL];
+  solve_W(g, W, F, M, scan, u);
 #pragma unroll
-  for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); U[sl] = (i < M.n) ? (double)W.u[i] : 0.0; }
+  for (int sl = 0; sl < NSL; ++sl) U[sl] = from_st(u[sl]);
   for (int it = 0; it < refine; ++it) {
 #pragma unroll
     for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) W.x[i] = U[sl]; }
@@ -802,15 +874,15 @@ __device__ __forceinline__ void stage_solve(const Grp<NW>& g, ModeMem<NW, NSL, S
 #pragma unroll
     for (int sl = 0; sl < NSL; ++sl) {
       const int i = comp_of<NW>(gt, sl);
-      if (i < M.n) W.r[i] = (ST)(b[sl] - (s * U[sl] - JU[sl]));  // s U - J U ≈ b first: rounding of order ε|b|, not ε|J U|
+      if (i < M.n) W.r[i] = to_st<ST>(b[sl] - (s * U[sl] - JU[sl]));  // s U - J U ≈ b first: rounding of order ε|b|, not ε|J U|
     }
     g.sync();
-    solve_W(g, W, F, M, scan);
+    solve_W(g, W, F, M, scan, u);
     float c = 0.0f;
 #pragma unroll
     for (int sl = 0; sl < NSL; ++sl) {
       const int i = comp_of<NW>(gt, sl);
-      if (i < M.n) { const ST d = W.u[i]; U[sl] += (double)d; c = fmaxf(c, fabsf((float)d) * isk[sl]); }
+      if (i < M.n) { const ST d = u[sl]; U[sl] += from_st(d); c = fmaxf(c, fabsf((float)d) * isk[sl]); }
     }
     if (it + 1 < refine || (it == 0 && first_correction)) {
       const float cm = group_max(g, W, c);
@@ -1059,9 +1131,12 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
       // the end point, 1/h, 1/(hγ), the step end and the stage times (FP64; every warp reads them).
       const int cw = NW > 1 ? 1 : 0;
       auto publish = [&](double hp, double tc) {
+        const bool done = !(tc < tend);
         if (tc + 1.01 * hp >= tend) hp = tend - tc;
         const double te = (hp == tend - tc) ? tend : tc + hp;
+        const bool tiny = !(hp > 1e-14 * tc);
         if (g.lane == 0) {
+          W.ctlf = (done ? 1 : 0) | (tiny ? 2 : 0);
           W.ctl[0] = hp; W.ctl[1] = 1.0 / hp; W.ctl[2] = 1.0 / (hp * TB::gam); W.ctl[3] = te;
 #pragma unroll
           for (int q = 1; q < TB::NTIME; ++q) {
@@ -1074,11 +1149,13 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         }
       };
       if (g.wq == cw) publish(h, t);
-      while (t < tend) {
+      for (;;) {
         g.sync();  // step control published; the previous step's readers of x and the coefficient sets are done
+        const int fl = W.ctlf;  // bit 0: t reached the end; bit 1: the step is below 1e-14 t
+        if (fl & 1) break;
         if (++iters > A.maxiters) { status = SBZ_MAXITERS; break; }
+        if (fl & 2) { status = nonfinite ? SBZ_NONFINITE : SBZ_DTMIN; break; }
         h = W.ctl[0];
-        if (!(h > 1e-14 * t)) { status = nonfinite ? SBZ_NONFINITE : SBZ_DTMIN; break; }
         const CSet& CJ = W.cs[sJ];
         const double ih = W.ctl[1], s = W.ctl[2], tn = W.ctl[3];
         // coefficient set of each later stage time: 1..NTIME-1 in place, the step end in sE
@@ -1090,10 +1167,11 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         // next step's Jacobian set), and the factorisation for this h
         coef_eval(g, W, tset + 1, W.ctl + 4, TB::NTIME, 1u << (TB::NTIME - 1), false, cd, tab, M.nexpr, M.nx, mk);
         factorize(g, W, F, CJ, comps, M, k, h, s, TB::gam, scan);
-        double U[TB::S][NSL], b[NSL], Fv[NSL], Y[NSL];
+        double b[NSL], Fv[NSL], Y[NSL], Ul[NSL];  // Ul: the last stage computed
+        double U[TB::S][NSL];
         float isk[NSL];  // refinement stopping weights
 #pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) isk[sl] = 1.0f / (float)(atol + rtol * fabs(y[sl]));
+        for (int sl = 0; sl < NSL; ++sl) isk[sl] = 1.0f / f64_to_f32(atol + rtol * fabs(y[sl]));
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = f0[sl] + h * TB::d(0) * ft[sl];
         float c1 = 1e30f;
@@ -1130,6 +1208,8 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
           }
           stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, U[st]);
         }
+#pragma unroll
+        for (int sl = 0; sl < NSL; ++sl) Ul[sl] = U[TB::S - 1][sl];
         // new state (stiffly accurate: y1 = last stage input + last stage) and the FP64 error norm
         // of the last stage (the stage solutions are FP64 after refinement; only the
         // factorisation was FP32)
@@ -1139,16 +1219,18 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
 #pragma unroll
           for (int sl = 0; sl < NSL; ++sl) {
             const int i = comp_of<NW>(gt, sl);
-            y1[sl] = Y[sl] + U[TB::S - 1][sl];
+            y1[sl] = Y[sl] + Ul[sl];
             if (i < n) {
-              const double sk = atol + rtol * fmax(fabs(y[sl]), fabs(y1[sl]));
-              const double q = U[TB::S - 1][sl] / sk;
+              const double sk = atol + rtol * __longlong_as_double(max(dkey(fabs(y[sl])), dkey(fabs(y1[sl]))));
+              const double q = Ul[sl] / sk;
               e2 += q * q;
             }
           }
           err2 = group_sum(g, W, e2) * inv_n;  // squared RMS error norm
         }
-        if (isfinite(err2) && err2 <= 1.0) {
+        // err2 >= 0: accepted when finite and at most 1, by its bit pattern (inf, NaN and any
+        // sign-bit pattern compare above 1 as unsigned)
+        if ((unsigned long long)dkey(err2) <= (unsigned long long)dkey(1.0)) {
           // accept: f(t1, y1) with the t1 coefficients, then dense output
 #pragma unroll
           for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < n) W.x[i] = y1[sl]; }
@@ -1168,7 +1250,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
           double f1[NSL];
           matvec_jd<NW, NSL>(g, W.x, W.cs[sE], comps, M, k, f1, ft);
           { const int tsw = sJ; sJ = sE; sE = tsw; }
-          if (taus && jout < A.ntau && taus[jout] <= tn) {
+          if (taus && jout < A.ntau && dkey(taus[jout]) <= dkey(tn)) {
             // continuous extension y(t + θh) = (1-θ) y + θ (y1 + (1-θ)(K0 + θ K1 + θ² K2))
             double K[TB::NDENSE][NSL];
 #pragma unroll
@@ -1181,7 +1263,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
                 K[r][sl] = v;
               }
             g.sync();  // x readers of the f1 product are done
-            while (jout < A.ntau && taus[jout] <= tn) {
+            while (jout < A.ntau && dkey(taus[jout]) <= dkey(tn)) {
               const double tau = taus[jout];
               const double th = (tau - t) / (tn - t), th1 = 1.0 - th;
               double yo[NSL];
@@ -1199,7 +1281,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         } else {
           ++nrej;
           rejected = true;
-          if (!isfinite(err2)) nonfinite = true;
+          if ((dkey(err2) & 0x7ff0000000000000ll) == 0x7ff0000000000000ll) nonfinite = true;  // inf or NaN
           if (g.wq == cw) publish(nonfinite ? 0.2 * h : h * fmax(0.2, 0.9 * exp(-0.5 * TB::rej * log(err2))), t);
           // J's coefficients (at t) and ∂f/∂τ stay valid; only the factorisation changes
         }

@@ -93,6 +93,7 @@ int build_cosmo(const Background& B, const ModelDesc& M, const sbz_model& m, Cos
   const Cosmo& P = B.P;
   D.tau_start = B.tau_start; D.tau0 = B.tau0; D.taurec = B.taurec;
   D.lnt0 = B.lnt0; D.idlnt = 1.0 / B.dlnt; D.ntab = B.ntab;
+  D.lnt0f = (float)D.lnt0; D.idlntf = (float)D.idlnt;
   D.Oc0 = P.Oc0; D.Ob0 = P.Ob0; D.Og0 = P.Og0; D.On0 = P.On0; D.wh = P.wh; D.y0 = P.y0;
   D.R0 = 4.0 / 3.0 * P.Og0 / P.Ob0; D.As = P.As; D.ns = P.ns; D.kpivot = P.kpivot;
   for (int j = 0; j < M.nx; ++j) { D.xq[j] = P.xq[j]; D.Wq[j] = P.Wq[j]; D.dlnf[j] = P.dlnf[j]; D.ixq[j] = 1.0 / P.xq[j]; }
