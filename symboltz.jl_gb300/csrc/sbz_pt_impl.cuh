@@ -47,6 +47,26 @@ constexpr int kNSets = TB::NTIME + 2;  // J (step start), the later stage times 
 
 static_assert(sizeof(ModelDesc) % 4 == 0 && sizeof(CompDesc) % 4 == 0 && sizeof(CosmoDesc) % 4 == 0, "word copies");
 
+// The tableau as a constant-memory table for the rolled stage loop of wide groups (stage index
+// uniform over the group: broadcast reads).
+struct RosTab {
+  double A[TB::S][TB::S], C[TB::S][TB::S], d[TB::S];
+  int tslot[TB::S], hasd[TB::S], incr[TB::S];
+  int nst;
+  constexpr RosTab() : A{}, C{}, d{}, tslot{}, hasd{}, incr{}, nst(TB::S) {
+    for (int i = 0; i < TB::S; ++i) {
+      for (int j = 0; j < TB::S; ++j) { A[i][j] = TB::A(i, j); C[i][j] = TB::C(i, j); }
+      d[i] = TB::d(i); tslot[i] = TB::tslot(i); hasd[i] = TB::d(i) != 0.0; incr[i] = TB::incremental(i);
+    }
+  }
+};
+static __constant__ RosTab kRos = RosTab();
+// Wide groups (four or more warps per mode: latency-bound spectra) run the stage loop rolled, one
+// copy of the stage body, so the step's code stays in the instruction cache; the stage solutions
+// then live in shared memory.  Narrow groups keep the unrolled loop with the stages in registers.
+template <int NW>
+constexpr bool kRolledStages = NW >= 4;
+
 // one coefficient set: operator coefficients, their τ-derivatives, functional weights
 struct CSet {
   double cv[kNCV], cvd[kNCV], w[kWF], wd[kWF];
@@ -69,6 +89,7 @@ struct ModeMem {
   ST hmul[kMaxChains], hcorr[kMaxChains];
   ST wS[kWF], fS[4];  // Jacobian-set functional weights and Φ̇ coefficients in solve precision
   CSet cs[kNSets];
+  double Us[kRolledStages<NW> ? TB::S : 1][kRolledStages<NW> ? NM : 1];  // stage solutions (rolled stage loop)
   double B[kMaxT][B_COUNT], dB[kMaxT][B_COUNT];
   double src[4];      // e^{-κ}, κ̈, κ⃛ at an output time
   double red[2][NW];  // ping-pong group reductions
@@ -1168,10 +1189,60 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         coef_eval(g, W, tset + 1, W.ctl + 4, TB::NTIME, 1u << (TB::NTIME - 1), false, cd, tab, M.nexpr, M.nx, mk);
         factorize(g, W, F, CJ, comps, M, k, h, s, TB::gam, scan);
         double b[NSL], Fv[NSL], Y[NSL], Ul[NSL];  // Ul: the last stage computed
-        double U[TB::S][NSL];
+        double U[kRolledStages<NW> ? 1 : TB::S][NSL];  // the stages (unrolled loop)
         float isk[NSL];  // refinement stopping weights
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) isk[sl] = 1.0f / f64_to_f32(atol + rtol * fabs(y[sl]));
+        if constexpr (kRolledStages<NW>) {
+          float c1 = 1e30f;
+          int rk = A.refine;
+          // the stage count read at run time: the compiler sees no fixed trip count to unroll or specialise
+          const int nst = *reinterpret_cast<const volatile int*>(&kRos.nst);
+#pragma unroll 1
+          for (int st = 0; st < nst; ++st) {
+            if (st == 0) {
+#pragma unroll
+              for (int sl = 0; sl < NSL; ++sl) b[sl] = f0[sl] + h * TB::d(0) * ft[sl];
+            } else {
+              // stage input: y + Σ A_st,j U_j, or the previous input plus U_{st-1}
+              const bool inc = kRos.incr[st] != 0;
+#pragma unroll
+              for (int sl = 0; sl < NSL; ++sl) {
+                const int i = comp_of<NW>(gt, sl);
+                double v;
+                if (inc) {
+                  v = Y[sl] + Ul[sl];
+                } else {
+                  v = y[sl];
+#pragma unroll 1
+                  for (int j = 0; j < st; ++j) v += kRos.A[st][j] * W.Us[j][i];
+                }
+                Y[sl] = v;
+                if (i < n) W.x[i] = v;
+              }
+              g.sync();
+              const int q = kRos.tslot[st];
+              matvec<NW, NSL>(g, W.x, W.cs[q < TB::NTIME ? q : sE], comps, M, k, Fv);
+              const bool hd = kRos.hasd[st] != 0;
+              const double hdst = h * kRos.d[st];
+#pragma unroll
+              for (int sl = 0; sl < NSL; ++sl) {
+                const int i = comp_of<NW>(gt, sl);
+                double cu = 0;
+#pragma unroll 1
+                for (int j = 0; j < st; ++j) cu += kRos.C[st][j] * W.Us[j][i];
+                b[sl] = Fv[sl] + ih * cu;
+                if (hd) b[sl] += hdst * ft[sl];
+              }
+            }
+            // lazy refinement: the later stages share stage 1's W; they are refined only when stage
+            // 1's first FP64 correction is at or above refine_skip (error-weight units)
+            stage_solve(g, W, F, CJ, comps, M, k, s, rk, scan, isk, b, Ul, st == 0 ? &c1 : nullptr);
+            if (st == 0) rk = (A.refine > 0 && c1 < A.refine_skip) ? 0 : A.refine;
+#pragma unroll
+            for (int sl = 0; sl < NSL; ++sl) W.Us[st][comp_of<NW>(gt, sl)] = Ul[sl];
+          }
+        } else {
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) b[sl] = f0[sl] + h * TB::d(0) * ft[sl];
         float c1 = 1e30f;
@@ -1210,6 +1281,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         }
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) Ul[sl] = U[TB::S - 1][sl];
+        }
         // new state (stiffly accurate: y1 = last stage input + last stage) and the FP64 error norm
         // of the last stage (the stage solutions are FP64 after refinement; only the
         // factorisation was FP32)
@@ -1259,7 +1331,13 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
               for (int sl = 0; sl < NSL; ++sl) {
                 double v = 0;
 #pragma unroll
-                for (int j = 0; j < TB::S; ++j) if (TB::dense(r, j) != 0.0) v += TB::dense(r, j) * U[j][sl];
+                for (int j = 0; j < TB::S; ++j) {
+                  if (TB::dense(r, j) == 0.0) continue;
+                  double uj;
+                  if constexpr (kRolledStages<NW>) uj = W.Us[j][comp_of<NW>(gt, sl)];
+                  else uj = U[j][sl];
+                  v += TB::dense(r, j) * uj;
+                }
                 K[r][sl] = v;
               }
             g.sync();  // x readers of the f1 product are done
