@@ -881,12 +881,30 @@ __device__ __forceinline__ void stage_solve(const Grp<NW>& g, ModeMem<NW, NSL, S
   const int gt = g.gt;
 #pragma unroll
   for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) W.r[i] = to_st<ST>(b[sl]); }
-  g.sync();
-  ST u[NSL];
-  solve_W(g, W, F, M, scan, u);
+  // one loop over the solve and its corrections, so the structured solve's code appears once
+  for (int it = 0;; ++it) {
+    g.sync();
+    ST u[NSL];
+    solve_W(g, W, F, M, scan, u);
+    if (it == 0) {
 #pragma unroll
-  for (int sl = 0; sl < NSL; ++sl) U[sl] = from_st(u[sl]);
-  for (int it = 0; it < refine; ++it) {
+      for (int sl = 0; sl < NSL; ++sl) U[sl] = from_st(u[sl]);
+    } else {
+      float c = 0.0f;
+#pragma unroll
+      for (int sl = 0; sl < NSL; ++sl) {
+        const int i = comp_of<NW>(gt, sl);
+        if (i < M.n) { const ST d = u[sl]; U[sl] += from_st(d); c = fmaxf(c, fabsf((float)d) * isk[sl]); }
+      }
+      const int r = it - 1;  // correction index
+      if (r + 1 < refine || (r == 0 && first_correction)) {
+        const float cm = group_max(g, W, c);
+        if (r == 0 && first_correction) *first_correction = cm;
+        if (r + 1 < refine && cm < 1e-3f) break;
+      }
+    }
+    if (it >= refine) break;
+    // residual b - W U in FP64 for the next correction
 #pragma unroll
     for (int sl = 0; sl < NSL; ++sl) { const int i = comp_of<NW>(gt, sl); if (i < M.n) W.x[i] = U[sl]; }
     g.sync();
@@ -896,19 +914,6 @@ __device__ __forceinline__ void stage_solve(const Grp<NW>& g, ModeMem<NW, NSL, S
     for (int sl = 0; sl < NSL; ++sl) {
       const int i = comp_of<NW>(gt, sl);
       if (i < M.n) W.r[i] = to_st<ST>(b[sl] - (s * U[sl] - JU[sl]));  // s U - J U ≈ b first: rounding of order ε|b|, not ε|J U|
-    }
-    g.sync();
-    solve_W(g, W, F, M, scan, u);
-    float c = 0.0f;
-#pragma unroll
-    for (int sl = 0; sl < NSL; ++sl) {
-      const int i = comp_of<NW>(gt, sl);
-      if (i < M.n) { const ST d = u[sl]; U[sl] += from_st(d); c = fmaxf(c, fabsf((float)d) * isk[sl]); }
-    }
-    if (it + 1 < refine || (it == 0 && first_correction)) {
-      const float cm = group_max(g, W, c);
-      if (it == 0 && first_correction) *first_correction = cm;
-      if (it + 1 < refine && cm < 1e-3f) break;
     }
   }
 }
