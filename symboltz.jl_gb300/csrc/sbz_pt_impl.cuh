@@ -217,6 +217,13 @@ __device__ __forceinline__ double from_st(float v) { return f32_to_f64(v); }
 __device__ __forceinline__ double from_st(double v) { return v; }
 // Order of non-negative doubles (and NaN above +inf) by their bit patterns: integer comparisons.
 __device__ __forceinline__ long long dkey(double v) { return __double_as_longlong(v); }
+// Max / min of doubles of either sign through an order-preserving integer key (no NaN operands).
+__device__ __forceinline__ long long okey(double v) {
+  const long long b = __double_as_longlong(v);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffll);
+}
+__device__ __forceinline__ double dmax(double a, double b) { return okey(a) >= okey(b) ? a : b; }
+__device__ __forceinline__ double dmin(double a, double b) { return okey(a) <= okey(b) ? a : b; }
 
 template <typename ST>
 __device__ __forceinline__ ST rcp(ST v);
@@ -1163,6 +1170,8 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         const bool tiny = !(hp > 1e-14 * tc);
         if (g.lane == 0) {
           W.ctlf = (done ? 1 : 0) | (tiny ? 2 : 0);
+          // 1/(hγ) divided as the oracle divides it: the FP64 refinement residuals use it, and a last-bit
+          // difference can move an accept/reject decision at the tolerance edge
           W.ctl[0] = hp; W.ctl[1] = 1.0 / hp; W.ctl[2] = 1.0 / (hp * TB::gam); W.ctl[3] = te;
 #pragma unroll
           for (int q = 1; q < TB::NTIME; ++q) {
@@ -1315,11 +1324,11 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
           if (g.wq == cw) {
             // PI controller fac = 0.9 err^-beta1 errold^beta2 (OrdinaryDiffEq's defaults for the
             // method's order), FP64 in both precisions; log(errold) is kept from the previous acceptance
-            const double lerr = 0.5 * log(fmax(err2, 1e-20));
+            const double lerr = 0.5 * log(dmax(err2, 1e-20));
             double fac = 0.9 * exp(-TB::beta1 * lerr + TB::beta2 * lerrold);
-            fac = fmin(10.0, fmax(0.2, fac));
-            if (rejected) fac = fmin(fac, 1.0);
-            lerrold = fmax(lerr, kLogErrFloor);
+            fac = dmin(10.0, dmax(0.2, fac));
+            if (rejected) fac = dmin(fac, 1.0);
+            lerrold = dmax(lerr, kLogErrFloor);
             publish(h * fac, tn);
           }
           // f(t1, y1) and the next step's ∂f/∂τ = (dJ/dτ)(t1) y1, both from the t1 coefficient set,
@@ -1365,7 +1374,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
           ++nrej;
           rejected = true;
           if ((dkey(err2) & 0x7ff0000000000000ll) == 0x7ff0000000000000ll) nonfinite = true;  // inf or NaN
-          if (g.wq == cw) publish(nonfinite ? 0.2 * h : h * fmax(0.2, 0.9 * exp(-0.5 * TB::rej * log(err2))), t);
+          if (g.wq == cw) publish(nonfinite ? 0.2 * h : h * dmax(0.2, 0.9 * exp(-0.5 * TB::rej * log(err2))), t);
           // J's coefficients (at t) and ∂f/∂τ stay valid; only the factorisation changes
         }
       }
