@@ -48,6 +48,9 @@ REFINE_SKIP_CL = 1e-2
 # divided by k²): at rtol 1e-6 every l is within 1.1e-4 of a converged solution for atol 1e-7 and
 # within 1.3e-5 for atol 3e-8 (oracle, Rodas5P, against rtol = atol = 1e-9).
 PT_RTOL, PT_ATOL = 1e-6, 3e-8
+# DRAM bytes (read + write) of the spectrum's perturbation launch: one ncu pass of
+# dram__bytes_read.sum + dram__bytes_write.sum on `bench.py --profile-case los` (4.15 MB + 2.53 MB)
+PT_LAUNCH_DRAM_BYTES = 6.68e6
 
 
 def workload_grids(S, prob):
@@ -206,6 +209,8 @@ def run_ours(args):
                                     normalization="Dl")
         accuracy["vs_fp64_gpu"] = rel_by_range(Dl, Dl64)
         accuracy["fp64_failed_modes"] = int(np.count_nonzero(st64))
+        # the all-FP64 kernel on the same modes (one untimed-loop call: CUDA-event phase time)
+        accuracy["fp64_perturbations_ms"] = round(float(S.timings(p64)["perturbations"]), 1)
     pconv = S.CosmologyProblem(M, PARAMS, precision="fp64", pt_rtol=1e-9, pt_atol=1e-9, maxiters=10**7)
     Dlc, stc = S.spectrum_cmb(["TT", "TE", "EE"], pconv, jl, lall, kinterp=kinterp, taus=taus, return_status=True,
                               normalization="Dl")
@@ -246,12 +251,12 @@ def run_ours(args):
                      # dram__bytes_read.sum + dram__bytes_write.sum of one full pt_kernel launch of this
                      # workload (ncu, profiles/launches_bench_lcdm_massive_nu.md): 1.98 MB + 2.66 MB; the
                      # coefficient tables stay in L1/L2, the kernel is FP64-latency bound
-                     "traffic": 4.64e6,
+                     "traffic": PT_LAUNCH_DRAM_BYTES,
                      "kernel": "pt_kernel (perturbation modes)", "flops_per_step": fl, "steps_per_launch": steps_total,
                      "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 entry in MEASURED_PEAKS.json)",
                      # the same launch against the HBM roofline: measured traffic over its CUDA-event time
-                     "hbm": {"achieved_gbs": round(4.64e6 / pt_avg / 1e9, 6), "peak_gbs": peaks.get("hbm_gbs"),
-                             "frac": round(4.64e6 / pt_avg / 1e9 / peaks["hbm_gbs"], 8) if peaks.get("hbm_gbs") else None}},
+                     "hbm": {"achieved_gbs": round(PT_LAUNCH_DRAM_BYTES / pt_avg / 1e9, 6), "peak_gbs": peaks.get("hbm_gbs"),
+                             "frac": round(PT_LAUNCH_DRAM_BYTES / pt_avg / 1e9 / peaks["hbm_gbs"], 8) if peaks.get("hbm_gbs") else None}},
         "accuracy": accuracy,
         "gpu_launches": int(K * 6),
         "clocks": ck.summary(),
@@ -333,7 +338,7 @@ def batched_workload(ncosmo=256, seed=0):
 
 def run_batched(args):
     """Batched P(k): every mode of every cosmology in one perturbation launch (Δm output), the
-    launch shape picked by the autotuner, mixed precision against all-FP64."""
+    launch shape picked by the autotuner for each precision, mixed precision against all-FP64."""
     import torch
     import symboltz as S
     assert torch.cuda.is_available(), "bench needs a GPU"
@@ -342,18 +347,15 @@ def run_batched(args):
     ks = np.concatenate([S.k_from_hMpc(S.loggrid(1e-5, 5.0, length=int(n))) for n in nks])
     cos = np.concatenate([np.full(int(n), i) for i, n in enumerate(nks)])
     ti = lambda k: np.minimum(1e-2 / k, 1e-4)  # noqa: E731  (spectrum_matter's rule, fourier.jl:76-81)
-    res, chosen = {}, {}
-    for prec in ("mixed", "fp64"):  # the FP64 run uses the launch shape tuned for the mixed run
+    res = {}
+    for prec in ("mixed", "fp64"):  # each precision runs the launch shape the autotuner picks for it
         skip = REFINE_SKIP_CL if prec == "mixed" else None
-        prob = S.CosmologyProblem(M, pars, precision=prec, pt_rtol=PT_RTOL, pt_atol=PT_ATOL, refine_skip=skip, **chosen)
+        prob = S.CosmologyProblem(M, pars, precision=prec, pt_rtol=PT_RTOL, pt_atol=PT_ATOL, refine_skip=skip)
         t0 = time.perf_counter()
         bg = prob.solvebg()
         t_bg = time.perf_counter() - t0
         assert np.all(bg.status == 0)
-        tune = None
-        if prec == "mixed":
-            tune = S.autotune(prob, ks, ti, output="delta_m", cosmo=cos)
-            chosen = dict(warps_per_mode=tune["warps_per_mode"], blocks_per_sm=tune["blocks_per_sm"])
+        tune = S.autotune(prob, ks, ti, output="delta_m", cosmo=cos)
         times = []
         for _ in range(max(1, args.steps)):
             t0 = time.perf_counter()
@@ -370,7 +372,8 @@ def run_batched(args):
                       "steps": res["mixed"]["steps"], "autotune": {"chosen": [res["mixed"]["tune"]["warps_per_mode"], res["mixed"]["tune"]["blocks_per_sm"]],
                                                                    "candidates_ms": {str(k): round(v, 1) for k, v in res["mixed"]["tune"]["candidates_ms"].items()}}},
             "fp64": {"s": round(res["fp64"]["s"], 3), "kmodes_per_s": round(n / res["fp64"]["s"], 1), "failed": res["fp64"]["failed"],
-                     "steps": res["fp64"]["steps"]},
+                     "steps": res["fp64"]["steps"], "autotune": {"chosen": [res["fp64"]["tune"]["warps_per_mode"], res["fp64"]["tune"]["blocks_per_sm"]],
+                                                                 "candidates_ms": {str(k): round(v, 1) for k, v in res["fp64"]["tune"]["candidates_ms"].items()}}},
             "speedup_mixed_over_fp64": round(res["fp64"]["s"] / res["mixed"]["s"], 3),
             "pk_rel_mixed_vs_fp64": {"max": float(rel.max()), "median": float(np.median(rel)), "max_k_ge_1e-4_hMpc": float(rel[hi].max())},
             "tolerances": {"pt_rtol": PT_RTOL, "pt_atol": PT_ATOL, "refine_skip_mixed": REFINE_SKIP_CL},
@@ -428,7 +431,7 @@ def run_surrogate(args):
         th = train[s0:s0 + 64]
         F, taus, vis, _ = sur.solve_factors(th)
         for c, t in enumerate(th):
-            X = sur.features(t, taus[c])
+            X = sur.features(t, taus[c], vis[c])
             Y = sur.to_targets(F[c], ks, vis[c]).reshape(-1, 7)
             idx = rng.choice(len(X), size=min(keep, len(X)), replace=False)
             SG.write_training_set(path, X[idx], Y[idx])

@@ -61,11 +61,13 @@ struct RosTab {
   }
 };
 static __constant__ RosTab kRos = RosTab();
-// Wide groups (four or more warps per mode: latency-bound spectra) run the stage loop rolled, one
-// copy of the stage body, so the step's code stays in the instruction cache; the stage solutions
-// then live in shared memory.  Narrow groups keep the unrolled loop with the stages in registers.
+// Groups of two or more warps run the stage loop rolled, one copy of the stage body, so the step's
+// code stays in the instruction cache (the unrolled loop streamed it: the 1000-mode spectrum went
+// from 1,788 to 1,721 ms with four-warp groups, the batched 256-cosmology solve from 80.7 to 65.1 s
+// with two-warp groups); the stage solutions then live in shared memory.  One-warp groups keep
+// the unrolled loop with the stages in registers (their shared memory sets the occupancy).
 template <int NW>
-constexpr bool kRolledStages = NW >= 4;
+constexpr bool kRolledStages = NW >= 2;
 
 // one coefficient set: operator coefficients, their τ-derivatives, functional weights
 struct CSet {

@@ -166,6 +166,7 @@ class SourceSurrogate:
     k² S_E = 3 v f4 / (16 χ²)  (src/models/cosmologies.jl:99-104)."""
 
     KPOW = np.array([0, 0, 1, 2, 0, 1, 2])  # factors are learned as f_j / k^KPOW[j]
+    NIN = 10  # inputs: θ (6), log k, log τ, sin and cos of the acoustic phase k r_s(τ)
 
     @property
     def net(self):
@@ -177,7 +178,7 @@ class SourceSurrogate:
         solver tolerances of the training data and of the fallback."""
         self.M, self.ks, self.ntau = M, np.asarray(ks, dtype=np.float64), ntau
         self.logk = (np.log(self.ks.min()), np.log(self.ks.max()))
-        self.nets = [MLP(8, width, nhidden, 7, batch, seed + 7919 * i) for i in range(max(1, members))]
+        self.nets = [MLP(self.NIN, width, nhidden, 7, batch, seed + 7919 * i) for i in range(max(1, members))]
         self.pt_rtol, self.pt_atol = pt_rtol, pt_atol
         self.mean = np.zeros(7)
         self.scale = np.ones(7)
@@ -185,19 +186,42 @@ class SourceSurrogate:
         self.env_la = np.zeros((2, 7))
 
     # ---- features, background, targets ------------------------------------------------------
-    def features(self, theta, taus, ks=None):
-        """[nk * ntau, 8] inputs for one cosmology: θ mapped to [-1, 1] by the box, log k and log τ to
-        [-1, 1]; row i*ntau + j is (k_i, τ_j)."""
+    def features(self, theta, taus, vis, ks=None):
+        """[nk * ntau, NIN] inputs for one cosmology: θ mapped to [-1, 1] by the box, log k and log τ to
+        [-1, 1], and the sine and cosine of the acoustic phase k r_s(τ) (r_s, the photon-baryon sound
+        horizon, is row 4 of vis), so the network does not have to build the acoustic oscillations
+        of the sources in k out of smooth functions; row i*ntau + j is (k_i, τ_j)."""
         ks = self.ks if ks is None else np.asarray(ks, dtype=np.float64)
         th = 2 * (np.asarray(theta) - BOX[:, 0]) / (BOX[:, 1] - BOX[:, 0]) - 1
         lk = 2 * (np.log(ks) - self.logk[0]) / (self.logk[1] - self.logk[0]) - 1
         lt = 2 * (np.log(taus) - LOGTAU[0]) / (LOGTAU[1] - LOGTAU[0]) - 1
         nk, nt = len(ks), len(taus)
-        X = np.empty((nk * nt, 8), dtype=np.float32)
+        X = np.empty((nk * nt, self.NIN), dtype=np.float32)
         X[:, :6] = th
         X[:, 6] = np.repeat(lk, nt)
         X[:, 7] = np.tile(lt, nk)
+        ph = np.outer(ks, vis[4]).ravel()
+        X[:, 8] = np.sin(ph)
+        X[:, 9] = np.cos(ph)
         return X
+
+    @staticmethod
+    def sound_horizon(bg, c, theta, taus):
+        """Photon-baryon sound horizon r_s(τ) = ∫ dτ' / sqrt(3 (1 + R)), R = 3 ω_b a / (4 ω_γ) (T0 =
+        2.7255 K, ω_γ = 2.4728e-5), from the background's a(τ) on 2048 log-spaced times (trapezoid;
+        r_s = τ/√3 before the first), at taus.  An input feature, so approximate is enough."""
+        p = box_params(theta)
+        wb = p["Omega_b"] * p["h"] ** 2
+        t = bg.t(c)
+        tf = np.geomspace(max(float(t[t > 0][0]), 1e-6), float(bg.tau0[c]), 2048)
+        a = bg.coefficients(tf, c)[:, 0]
+        cs = 1.0 / np.sqrt(3.0 * (1.0 + 0.75 * wb / 2.4728e-5 * a))
+        rs = tf[0] / np.sqrt(3.0) + np.concatenate([[0.0], np.cumsum(0.5 * (cs[1:] + cs[:-1]) * np.diff(tf))])
+        return np.interp(taus, tf, rs)
+
+    def background_rows(self, bg, c, theta, taus):
+        """v, v̇, v̈, e^{-κ} and r_s on taus: the rows of vis."""
+        return np.vstack([self.visibility(bg.coefficients(taus, c)), self.sound_horizon(bg, c, theta, taus)[None]])
 
     @staticmethod
     def visibility(coef):
@@ -222,7 +246,7 @@ class SourceSurrogate:
 
     def solve_factors(self, thetas, precision="mixed", ks=None):
         """Solver factors [ncos][nk][ntau][7] on (ks or the coarse grid) × each cosmology's τ grid,
-        with taus [ncos][ntau], visibilities [ncos][4][ntau] and the problem."""
+        with taus [ncos][ntau], background rows [ncos][5][ntau] (v, v̇, v̈, e^{-κ}, r_s) and the problem."""
         from . import CosmologyProblem, solvept
         ks = self.ks if ks is None else np.asarray(ks, dtype=np.float64)
         prob = CosmologyProblem(self.M, [box_params(t) for t in thetas], precision=precision, pt_rtol=self.pt_rtol,
@@ -236,11 +260,11 @@ class SourceSurrogate:
         out, st, _ = solvept(prob, np.tile(ks, len(thetas)), prob.opts.tau_ini, saveat=taus, output="factors", cosmo=cos)
         if np.any(st != 0):
             raise L.SbzError(f"{int(np.count_nonzero(st))} modes failed")
-        vis = np.stack([self.visibility(bg.coefficients(taus[c], c)) for c in range(len(thetas))])
+        vis = np.stack([self.background_rows(bg, c, thetas[c], taus[c]) for c in range(len(thetas))])
         return out.reshape(len(thetas), nk, self.ntau, 7), taus, vis, prob
 
     def backgrounds(self, thetas):
-        """Times [ncos][ntau], visibilities [ncos][4][ntau] and the problem of the given parameter
+        """Times [ncos][ntau], background rows [ncos][5][ntau] (v, v̇, v̈, e^{-κ}, r_s) and the problem of the given parameter
         points from their backgrounds alone (no perturbation modes solved)."""
         from . import CosmologyProblem
         prob = CosmologyProblem(self.M, [box_params(t) for t in thetas], pt_rtol=self.pt_rtol, pt_atol=self.pt_atol)
@@ -248,7 +272,7 @@ class SourceSurrogate:
         if np.any(bg.status != 0):
             raise L.SbzError("background failed for a cosmology of the box")
         taus = np.stack([cmb_taus(bg.t(c), bg.tau0[c], self.ntau) for c in range(len(thetas))])
-        vis = np.stack([self.visibility(bg.coefficients(taus[c], c)) for c in range(len(thetas))])
+        vis = np.stack([self.background_rows(bg, c, thetas[c], taus[c]) for c in range(len(thetas))])
         return taus, vis, prob
 
     def weights(self, vis):
@@ -271,7 +295,7 @@ class SourceSurrogate:
     @staticmethod
     def sources(F, ks, taus, vis):
         """(k S_T, k² S_E, S_ψ = 0) [nk][ntau][3] from factors; zero at χ = 0 (angular.jl:296)."""
-        v, vd, vdd, ek = (x[None, :] for x in vis)
+        v, vd, vdd, ek = (x[None, :] for x in vis[:4])
         k = ks[:, None]
         f = [F[..., j] for j in range(7)]
         sT = v * f[0] + ek * f[1] + (vd * f[2] + v * f[3]) / k**2 + 3.0 / (16.0 * k**2) * (vdd * f[4] + 2 * vd * f[5] + v * f[6])
@@ -285,7 +309,7 @@ class SourceSurrogate:
     def dataset(self, thetas):
         """(X, Y, taus) training arrays from the solver for the given parameter points."""
         F, taus, vis, _ = self.solve_factors(thetas)
-        X = np.concatenate([self.features(t, taus[c]) for c, t in enumerate(thetas)])
+        X = np.concatenate([self.features(t, taus[c], vis[c]) for c, t in enumerate(thetas)])
         Y = np.concatenate([self.to_targets(F[c], self.ks, vis[c]).reshape(-1, 7) for c in range(len(thetas))])
         return X, Y, taus
 
@@ -335,7 +359,7 @@ class SourceSurrogate:
     def predict_factors(self, theta, taus, vis, ks=None, member=None):
         """Factors from one member's network, or from the members' mean (member None)."""
         ks = self.ks if ks is None else np.asarray(ks, dtype=np.float64)
-        X = self.features(theta, taus, ks)
+        X = self.features(theta, taus, vis, ks)
         nets = self.nets if member is None else [self.nets[member]]
         Z = np.mean([net.infer(X).astype(np.float64) for net in nets], axis=0)
         G = ((Z * self.scale + self.mean) * self.envelope(X[:, 6])).reshape(len(ks), len(taus), 7)

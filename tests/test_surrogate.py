@@ -81,7 +81,7 @@ def test_surrogate_sources_through_the_line_of_sight_with_fallback():
     sur = SourceSurrogate(M, ks, ntau=48, width=128, nhidden=2, batch=1024, seed=3)
     train = sample_box(4, seed=0)
     X, Y, _ = sur.dataset(train)
-    assert X.shape == (4 * 32 * 48, 8) and Y.shape == (4 * 32 * 48, 7) and np.all(np.isfinite(Y))
+    assert X.shape == (4 * 32 * 48, SourceSurrogate.NIN) and Y.shape == (4 * 32 * 48, 7) and np.all(np.isfinite(Y))
     sur.fit(X, Y, steps=1, lr=1e-4)
     before = sur.mse(X, Y)
     sur.fit(X, Y, steps=400, lr=2e-3, lr_final=2e-4, chunks=4)
