@@ -61,13 +61,15 @@ struct RosTab {
   }
 };
 static __constant__ RosTab kRos = RosTab();
-// Groups of two or more warps run the stage loop rolled, one copy of the stage body, so the step's
-// code stays in the instruction cache (the unrolled loop streamed it: the 1000-mode spectrum went
-// from 1,788 to 1,721 ms with four-warp groups, the batched 256-cosmology solve from 80.7 to 65.1 s
-// with two-warp groups); the stage solutions then live in shared memory.  One-warp groups keep
-// the unrolled loop with the stages in registers (their shared memory sets the occupancy).
-template <int NW>
-constexpr bool kRolledStages = NW >= 2;
+// Groups of four or more warps, and two-warp groups in mixed precision, run the stage loop rolled,
+// one copy of the stage body, so the step's code stays in the instruction cache (the unrolled loop
+// streamed it: the 1000-mode spectrum went from 1,788 to 1,721 ms with four-warp groups, the
+// batched 256-cosmology solve from 80.7 to 65.1 s with two-warp groups); the stage solutions then
+// live in shared memory.  Narrower groups keep the unrolled loop with the stages in registers:
+// there shared memory sets the occupancy (the all-FP64 two-warp batch ran 119 s unrolled against
+// 150 s for the best rolled shape).
+template <int NW, typename ST>
+constexpr bool kRolledStages = NW >= 4 || (NW >= 2 && sizeof(ST) == 4);
 
 // one coefficient set: operator coefficients, their τ-derivatives, functional weights
 struct CSet {
@@ -91,7 +93,7 @@ struct ModeMem {
   ST hmul[kMaxChains], hcorr[kMaxChains];
   ST wS[kWF], fS[4];  // Jacobian-set functional weights and Φ̇ coefficients in solve precision
   CSet cs[kNSets];
-  double Us[kRolledStages<NW> ? TB::S : 1][kRolledStages<NW> ? NM : 1];  // stage solutions (rolled stage loop)
+  double Us[kRolledStages<NW, ST> ? TB::S : 1][kRolledStages<NW, ST> ? NM : 1];  // stage solutions (rolled stage loop)
   double B[kMaxT][B_COUNT], dB[kMaxT][B_COUNT];
   double src[4];      // e^{-κ}, κ̈, κ⃛ at an output time
   double red[2][NW];  // ping-pong group reductions
@@ -1205,11 +1207,11 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
         coef_eval(g, W, tset + 1, W.ctl + 4, TB::NTIME, 1u << (TB::NTIME - 1), false, cd, tab, M.nexpr, M.nx, mk);
         factorize(g, W, F, CJ, comps, M, k, h, s, TB::gam, scan);
         double b[NSL], Fv[NSL], Y[NSL], Ul[NSL];  // Ul: the last stage computed
-        double U[kRolledStages<NW> ? 1 : TB::S][NSL];  // the stages (unrolled loop)
+        double U[kRolledStages<NW, ST> ? 1 : TB::S][NSL];  // the stages (unrolled loop)
         float isk[NSL];  // refinement stopping weights
 #pragma unroll
         for (int sl = 0; sl < NSL; ++sl) isk[sl] = 1.0f / f64_to_f32(atol + rtol * fabs(y[sl]));
-        if constexpr (kRolledStages<NW>) {
+        if constexpr (kRolledStages<NW, ST>) {
           float c1 = 1e30f;
           int rk = A.refine;
           // the stage count read at run time: the compiler sees no fixed trip count to unroll or specialise
@@ -1350,7 +1352,7 @@ __device__ void pt_body(const PtArgs& A, const ModelDesc& M, const CompDesc* __r
                 for (int j = 0; j < TB::S; ++j) {
                   if (TB::dense(r, j) == 0.0) continue;
                   double uj;
-                  if constexpr (kRolledStages<NW>) uj = W.Us[j][comp_of<NW>(gt, sl)];
+                  if constexpr (kRolledStages<NW, ST>) uj = W.Us[j][comp_of<NW>(gt, sl)];
                   else uj = U[j][sl];
                   v += TB::dense(r, j) * uj;
                 }
