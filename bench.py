@@ -505,7 +505,7 @@ def run_surrogate(args):
                          "tflops": round(len(sur.nets) * steps * flops_step / t_train / 1e12, 1), "batch": 65536,
                          "loss_first_last": [losses[0][0], losses[0][-1]], "mse_train_standardised": mse_train,
                          "pk_surrogate": {"cosmologies": args.pk_train_cosmologies, "k": len(kpk), "s": round(t_pk, 2)}},
-            "model": "MLP 8 -> 4x512 SiLU -> 7 (perturbation factors) x 2 members, BF16 tcgen05 GEMMs, FP32 accumulate, Adam"}
+            "model": f"MLP {SG.SourceSurrogate.NIN} -> 4x512 SiLU -> 7 (perturbation factors) x 2 members, BF16 tcgen05 GEMMs, FP32 accumulate, Adam"}
     peaks = measured_peaks()
     nbytes = mlp_step_bytes()
     sps = t_train / (len(sur.nets) * steps)
