@@ -25,7 +25,10 @@
 // pipe for ~64 cycles, so a single mode's step latency is set by the FP64 instruction count per
 // warp; NW = 4 spreads one mode over the four sub-partitions of an SM, which is what bounds the
 // slowest (high-k) modes of a spectrum.  The group synchronises with a named barrier (NW > 1) or
-// __syncwarp (NW = 1); every barrier sits in group-uniform control flow.  Loops are bounded by
+// __syncwarp (NW = 1); every barrier sits in group-uniform control flow.  Step control (the PI
+// controller, 1/h, 1/(hγ), the stage times) runs on one warp and reaches the others through shared
+// memory at the loop-top barrier.  Wide groups run the stage loop rolled with the stage vectors in
+// shared memory (kRolledStages), narrow ones unrolled with them in registers.  Loops are bounded by
 // opts.maxiters and a step-size floor, so a mode that cannot finish sets a status code and the
 // group moves on.
 #include <cuda_runtime.h>

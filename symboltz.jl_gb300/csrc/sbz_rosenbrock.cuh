@@ -4,8 +4,8 @@
 //   W U_i = f(t + c_i h, y + Σ_j A_ij U_j) + Σ_j (C_ij / h) U_j + h d_i ∂f/∂τ,
 //   y1 = y + Σ_j m_j U_j,  error estimate = U_S (the embedded solution omits the last stage).
 // Step-size control: fac = 0.9 err^-beta1 errold^beta2 on acceptance, max(0.2, 0.9 err^-rej) on
-// rejection.  Accessors are constexpr and every kernel loop over stages is unrolled, so the
-// coefficients are immediates (zero entries fold away).
+// rejection.  Accessors are constexpr: unrolled stage loops see the coefficients as immediates (zero
+// entries fold away); rolled ones read a constant-memory copy built from the same accessors.
 //
 // Rodas5P (Steinebach 2023, order 5(4), stiffly accurate) is the reference's default integrator
 // (src/solve.jl:320,339; OrdinaryDiffEqRosenbrock).  Its dense output here is an order-4
