@@ -541,7 +541,11 @@ class SphericalBesselCache:
     """SphericalBesselCache(ls; xmax = 20 ls[end], dx = 2π/15, hermite) (angular.jl:18-26), on the GPU."""
 
     def __init__(self, ls, *, xmax=None, dx=2 * np.pi / 15, hermite=True):
-        self.l = L.i32(ls)
+        la = np.asarray(ls, dtype=np.float64)
+        if la.size == 0 or np.any(la != np.round(la)) or np.any(la < 0):
+            raise ValueError("SphericalBesselCache: the multipoles must be non-negative integers "
+                             "(non-integer l, which the reference's cache also accepts, is not supported)")
+        self.l = L.i32(la)
         self.xmax = float(20 * self.l[-1] if xmax is None else xmax)
         self.dx = dx
         h = C.c_void_p()

@@ -222,3 +222,13 @@ def test_training_set_file_round_trip(tmp_path):
     bad.write_bytes(b"SBZMLP01" + bytes(16))
     with pytest.raises(_lib.SbzError):
         SG.training_set_info(bad)
+
+
+def test_bessel_cache_rejects_non_integer_multipoles():
+    """The cache tabulates integer l (one recurrence in l per x); non-integer l, which the
+    reference's SphericalBesselCache also accepts (test/runtests.jl:903-913), fails loudly instead of
+    being truncated."""
+    import symboltz as S
+    for bad in (S.loggrid(2, 2500, length=100), [2, 3.5], [-1, 2], []):
+        with pytest.raises(ValueError, match="non-negative integers"):
+            S.SphericalBesselCache(bad)
