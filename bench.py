@@ -403,7 +403,7 @@ def run_surrogate(args):
     Training: scrambled-Sobol cosmologies of the box, solved in shards of 64 by the batched GPU
     solver at the workload's tolerances (perturbation factors on 400 k over 1e-4..0.5 h/Mpc × 500 τ),
     a random subset of each cosmology's points streamed into a flat SBZTRN01 training-set file, two
-    MLP members (8 → 4×512 SiLU → 7, BF16 tcgen05 GEMMs, FP32 accumulation, Adam, batch 65536)
+    MLP members (10 → 4×512 SiLU → 7, BF16 tcgen05 GEMMs, FP32 accumulation, Adam, batch 65536)
     trained from it; a P(k) surrogate (θ, log k → ln Δ_m², 1e-4..10 h/Mpc) trained on the solver's
     Δ_m.  Held-out accuracy: D_l TT/TE/EE to l = 2500 of held-out cosmologies against the all-FP64
     solver on the same grids, the surrogate alone and with fallback.  Mixed workload: cosmologies
@@ -551,7 +551,7 @@ def profile_case(args):
     """Small cases for ncu section captures, at the workload's tolerances and refinement threshold.  pt: 64 of the 1000 modes
     (even in log k, the slowest included), sources on 200 times.  los: one spectrum_cmb of the full workload (the line-of-sight
     kernel runs once on the full fine k grid; ~1.5 GB on the device).  mlp: the surrogate's training
-    step (8 -> 4x512 -> 7, batch 65536) on 2 M synthetic samples, one eager step, the graph capture
+    step (8 -> 4x512 -> 7, batch 65536; the same GEMM shapes as the 10-input surrogate, inputs padded to 64) on 2 M synthetic samples, one eager step, the graph capture
     and 4 graph replays, plus a timed run of 200 steps printed first."""
     import symboltz as S
     if args.profile_case == "mlp":
